@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Benchmark: batched kNN (k=5) on a 1M-point map, 100k-query batches.
+
+One step = one batch of 100k Nearest_Search queries (k = 5, max_dist = inf)
+against a 1M-point map (uniform in [-50, 50]^3, float32, seeded synthetic data).
+
+  value  - queries/s with the queries already in HBM (ikdg_knn_device), timed
+           with CUDA events on the tree's stream; L2 is flushed (512 MB write)
+           before every timed step, outside the events.
+  e2e    - the same metric through the host C ABI (ikdg_knn): host queries in,
+           ids + squared distances + points out, copies included.
+  roofline - the kNN kernel against the measured HBM copy bandwidth, with the
+           algorithmic bytes per query 12 + 8k + 16*32 + 32*ceil(log2(N/32)).
+  update_ms_per_scan - Add_Points(20k points, 0.5 m voxel downsampling) plus a
+           Delete_Point_Boxes call, per simulated scan, through the host API.
+  cpu_baseline - the CPU restatement of the reference (oracle port) on this
+           host's cores, same map and queries.
+
+`--impl reference` times that CPU implementation alone on the same workload.
+Multi-GPU (torchrun): every rank holds its own replica of the tree (the path
+does not shard); value is the sum over ranks, timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ikd-tree_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG)
+
+N_MAP = 1_000_000
+N_Q = 100_000
+K = 5
+EXTENT = 50.0
+MAP_SEED = 1002
+SCAN_POINTS = 20_000
+DS = 0.5
+WORKLOAD = "knn_k5_map1M_uniform_q100k"
+METRIC = "kNN queries/sec (k=5, 1M map)"
+
+
+def bytes_per_query(n: int, k: int) -> int:
+    depth = math.ceil(math.log2(n / 32))
+    return 12 + 8 * k + 16 * 32 + 32 * depth
+
+
+def make_map() -> np.ndarray:
+    return np.random.default_rng(MAP_SEED).uniform(-EXTENT, EXTENT, (N_MAP, 3)).astype(np.float32)
+
+
+def make_queries(step: int) -> np.ndarray:
+    return np.random.default_rng(7000 + step).uniform(-EXTENT, EXTENT, (N_Q, 3)).astype(np.float32)
+
+
+def make_scan(step: int):
+    """A 20k-point scan around a pose moving 1 m per scan, plus one delete box."""
+    rng = np.random.default_rng(9000 + step)
+    pose = np.array([-30.0 + step, 0.0, 0.0])
+    pts = (pose + rng.uniform(-20, 20, (SCAN_POINTS, 3))).astype(np.float32)
+    c = rng.uniform(-EXTENT, EXTENT, 3)
+    box = np.concatenate([c - 2.5, c + 2.5]).astype(np.float32).reshape(1, 6)
+    return pts, box
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def knn_traffic():
+    """Per-launch DRAM bytes of the kNN kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "knn_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    def __init__(self, device: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        fields = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={fields}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(pts, queries, steps: int):
+    """The oracle port (CPU restatement of the reference) on all host cores."""
+    sys.path.insert(0, ORACLE)
+    import oracle_lib
+    if not oracle_lib.available("port"):
+        oracle_lib.build("port")
+    cores = os.cpu_count() or 1
+    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind="port")
+    t.Build(pts)
+    t.knn(queries[0][:1000], K, nthreads=cores)
+    times = []
+    for s in range(steps):
+        t0 = time.perf_counter()
+        t.knn(queries[s % len(queries)], K, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    # Scan update on one core (mutations are single-caller in the reference).
+    upd = []
+    for s in range(3):
+        scan, box = make_scan(s)
+        t0 = time.perf_counter()
+        t.Add_Points(scan, True)
+        t.Delete_Point_Boxes(box)
+        upd.append(time.perf_counter() - t0)
+    t.close()
+    qps = N_Q / statistics.median(times)
+    return {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries",
+            "update_ms_per_scan": 1e3 * statistics.median(upd)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    pts = make_map()
+    steps = max(1, min(args.steps, 5))
+    queries = [make_queries(s) for s in range(steps)]
+    cb = cpu_baseline(pts, queries, steps)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * N_Q / cb["value"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K,
+                   "max_dist": "inf"},
+        "impl": "reference",
+        "cpu_baseline": {"value": cb["value"], "unit": "queries/s", "cores": cb["cores"], "kind": cb["kind"],
+                         "sample": cb["sample"]},
+        "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "update_ms_per_scan": cb["update_ms_per_scan"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import ikdg
+
+    world, rank, local = dist_env()
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("gloo")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    tree = ikdg.KDTree(0.5, 0.6, DS, device=local)
+    pts = make_map()
+    tree.Build(pts)
+    stream = torch.cuda.ExternalStream(tree.stream(), device=dev)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)  # 512 MB > L2
+    W, Kst = args.warmup, args.steps
+    qhost = [make_queries(s) for s in range(W + Kst)]
+    qdev = [torch.from_numpy(q).to(dev) for q in qhost]
+    ids = torch.empty((N_Q, K), dtype=torch.int32, device=dev)
+    d2 = torch.empty((N_Q, K), dtype=torch.float32, device=dev)
+    xyz = torch.empty((N_Q, K, 3), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def dev_step(s):
+        tree.knn_device(qdev[s].data_ptr(), N_Q, K, math.inf, ids.data_ptr(), d2.data_ptr(), xyz.data_ptr())
+
+    for s in range(W):
+        dev_step(s)
+    tree.synchronize()
+
+    # ---- value: device-resident queries, per-step CUDA events on the tree stream
+    barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    evs = []
+    t_wall0 = time.perf_counter()
+    for s in range(Kst):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dev_step(W + s)
+            e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = statistics.mean(step_ms)
+
+    # ---- e2e: host buffers through ikdg_knn (H2D + kernel + D2H inside)
+    for s in range(W):
+        tree.knn(qhost[s], K, math.inf)
+    e2e_ms = []
+    for s in range(Kst):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tree.knn(qhost[W + s], K, math.inf)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_step = statistics.mean(e2e_ms)
+
+    # ---- per-scan update latency (host API, synchronous)
+    upd = []
+    for s in range(max(3, min(Kst, 10))):
+        scan, box = make_scan(s)
+        t0 = time.perf_counter()
+        tree.Add_Points(scan, True)
+        tree.Delete_Point_Boxes(box)
+        upd.append(1e3 * (time.perf_counter() - t0))
+
+    # ---- aggregate over ranks (max time, summed throughput)
+    if world > 1:
+        t = torch.tensor([ms, e2e_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_step = float(t[0]), float(t[1])
+    value = world * N_Q / (ms / 1e3)
+    e2e_value = world * N_Q / (e2e_step / 1e3)
+    peak, peak_kind = measured_peak()
+    achieved = N_Q * bytes_per_query(N_MAP, K) / (ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": Kst, "warmup": W,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K, "max_dist": "inf",
+                   "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "queries/s", "ms_per_step": e2e_step,
+                "h2d_bytes_per_step": N_Q * 12, "d2h_bytes_per_step": N_Q * K * (4 + 4 + 12 + 0) + N_Q * 4},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": knn_traffic(), "peak_source": peak_kind,
+                     "bytes_per_query": bytes_per_query(N_MAP, K)},
+        "clocks": clocks,
+        "gpu_launches": 2 * Kst,
+        "update_ms_per_scan": statistics.median(upd),
+        "wall_s_timed_region": t_wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(pts, qhost[:3], 3)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    tree.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

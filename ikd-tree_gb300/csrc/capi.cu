@@ -1,0 +1,934 @@
+// Host side of libikdg: the tree object that owns the device pools, the
+// per-call orchestration of the kernels, and the extern "C" entry points
+// declared in include/ikdg.h.
+//
+// Every call runs on the tree's CUDA stream.  Host-pointer calls copy their
+// inputs in, run the kernels, copy the results out and synchronise; the
+// reference API is synchronous (it returns counts), so are these.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ikdg.h"
+#include "kernels.cuh"
+#include "update.cuh"
+
+namespace ikdg {
+namespace {
+
+struct CudaFail {
+    cudaError_t e;
+    const char* what;
+};
+struct Internal {
+    std::string what;
+};
+struct BadArg {
+    std::string what;
+};
+struct CapacityFail {
+    std::string what;
+};
+
+#define CK(x)                                        \
+    do {                                             \
+        cudaError_t _e = (x);                        \
+        if (_e != cudaSuccess) throw ::ikdg::CudaFail{_e, #x}; \
+    } while (0)
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Grow-only device buffer.
+struct Arena {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t need, cudaStream_t s) {
+        if (need <= bytes) return;
+        if (p != nullptr) {
+            CK(cudaStreamSynchronize(s));
+            CK(cudaFree(p));
+            p = nullptr;
+            bytes = 0;
+        }
+        size_t nb = std::max(need, (size_t)1 << 20);
+        CK(cudaMalloc(&p, nb));
+        bytes = nb;
+    }
+    void release() {
+        if (p != nullptr) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+// Sequential sub-allocation inside an arena.
+struct Carver {
+    char* base;
+    size_t off = 0;
+    explicit Carver(void* b) : base((char*)b) {}
+    template <class T>
+    T* take(size_t count) {
+        T* r = (T*)(base + off);
+        off += align_up(sizeof(T) * std::max<size_t>(count, 1));
+        return r;
+    }
+};
+
+// Squared-distance gate of Search (ikd_Tree.cpp:872-873, :887): the reference
+// compares a float distance against max_dist * max_dist in double.  For float
+// d, (double)d <= m2  <=>  d <= the largest float not above m2.
+float max_sq_threshold(double max_dist) {
+    double m2 = max_dist * max_dist;
+    if (std::isnan(m2)) return NAN;
+    if (std::isinf(m2)) return INFINITY;
+    float f = (float)m2;
+    if ((double)f > m2) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+template <class T>
+void grow_array(T*& p, size_t old_n, size_t new_n, int fill_byte, cudaStream_t s) {
+    T* q = nullptr;
+    CK(cudaMalloc(&q, sizeof(T) * std::max<size_t>(new_n, 1)));
+    if (fill_byte >= 0) CK(cudaMemsetAsync(q, fill_byte, sizeof(T) * new_n, s));
+    if (p != nullptr && old_n > 0) CK(cudaMemcpyAsync(q, p, sizeof(T) * old_n, cudaMemcpyDeviceToDevice, s));
+    if (p != nullptr) {
+        CK(cudaStreamSynchronize(s));
+        CK(cudaFree(p));
+    }
+    p = q;
+}
+
+template <class T>
+void free_array(T*& p) {
+    if (p != nullptr) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct Tree {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    float del_param = 0.5f, bal_param = 0.6f, ds_size = 0.2f;
+    int fill = 16;
+    int min_size = 2 * LEAF_CAP;
+
+    DevTree dt{};
+    UpdateAux aux{};
+    DevStatus* st_dev = nullptr;
+    DevStatus* st = nullptr;  // pinned host mirror
+    Arena op, bld, small;
+    float4* removed = nullptr;
+    long long removed_cap = 0;
+    long long next_id = 0;
+    int list_cap = 0;
+
+    std::mutex mu;
+    std::string err;
+
+    // ---- lifetime -------------------------------------------------------------
+    void init(int dev) {
+        device = dev;
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+        CK(cudaMalloc(&st_dev, sizeof(DevStatus)));
+        CK(cudaMallocHost(&st, sizeof(DevStatus)));
+        std::memset(st, 0, sizeof(DevStatus));
+        CK(cudaMemsetAsync(st_dev, 0, sizeof(DevStatus), stream));
+        dt.st = st_dev;
+        ensure_pools(64, 64);
+        reset_tree();
+        CK(cudaStreamSynchronize(stream));
+    }
+
+    void destroy() {
+        if (stream != nullptr) cudaStreamSynchronize(stream);
+        free_array(dt.node);
+        free_array(dt.ncnt);
+        free_array(dt.nparent);
+        free_array(dt.nheight);
+        free_array(dt.pts);
+        free_array(dt.leaf_n);
+        free_array(dt.lparent);
+        free_array(dt.free_node);
+        free_array(dt.free_leaf);
+        free_array(aux.pend);
+        free_array(aux.arrive);
+        free_array(aux.viol_flag);
+        free_array(aux.job_of_node);
+        free_array(aux.node_job);
+        free_array(aux.dirty_flag);
+        free_array(aux.job_of_leaf);
+        free_array(aux.leaf_job);
+        free_array(aux.items);
+        free_array(aux.viol);
+        free_array(aux.jobs);
+        free_array(aux.job_link);
+        free_array(aux.job_count);
+        free_array(aux.job_off);
+        free_array(aux.job_fill);
+        free_array(removed);
+        op.release();
+        bld.release();
+        small.release();
+        if (st_dev != nullptr) cudaFree(st_dev);
+        if (st != nullptr) cudaFreeHost(st);
+        st_dev = nullptr;
+        st = nullptr;
+        if (own_stream && stream != nullptr) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    // ---- pools -----------------------------------------------------------------
+    void ensure_pools(long long need_nodes, long long need_leaves) {
+        int old_n = dt.node_cap, old_l = dt.leaf_cap;
+        if (need_nodes > INT32_MAX / 2 || need_leaves > INT32_MAX / 2) throw CapacityFail{"tree too large"};
+        int new_n = old_n, new_l = old_l;
+        if (need_nodes > old_n) new_n = (int)std::max<long long>(need_nodes, (long long)old_n * 3 / 2);
+        if (need_leaves > old_l) new_l = (int)std::max<long long>(need_leaves, (long long)old_l * 3 / 2);
+        if (new_n != old_n) {
+            grow_array(dt.node, (size_t)old_n * 4, (size_t)new_n * 4, -1, stream);
+            grow_array(dt.ncnt, old_n, new_n, 0, stream);
+            grow_array(dt.nparent, old_n, new_n, 0xff, stream);
+            grow_array(dt.nheight, old_n, new_n, 0, stream);
+            grow_array(dt.free_node, old_n, new_n, -1, stream);
+            grow_array(aux.pend, old_n, new_n, 0, stream);
+            grow_array(aux.arrive, old_n, new_n, 0, stream);
+            grow_array(aux.viol_flag, old_n, new_n, 0, stream);
+            grow_array(aux.job_of_node, old_n, new_n, 0xff, stream);
+            grow_array(aux.node_job, old_n, new_n, 0xff, stream);
+            dt.node_cap = new_n;
+        }
+        if (new_l != old_l) {
+            grow_array(dt.pts, (size_t)old_l * LEAF_CAP, (size_t)new_l * LEAF_CAP, -1, stream);
+            grow_array(dt.leaf_n, old_l, new_l, 0, stream);
+            grow_array(dt.lparent, old_l, new_l, 0xff, stream);
+            grow_array(dt.free_leaf, old_l, new_l, -1, stream);
+            grow_array(aux.dirty_flag, old_l, new_l, 0, stream);
+            grow_array(aux.job_of_leaf, old_l, new_l, 0xff, stream);
+            grow_array(aux.leaf_job, old_l, new_l, 0xff, stream);
+            dt.leaf_cap = new_l;
+        }
+        int need_list = dt.node_cap + dt.leaf_cap + 2;
+        if (need_list > list_cap) {
+            grow_array(aux.items, list_cap, need_list, -1, stream);
+            grow_array(aux.viol, list_cap, need_list, -1, stream);
+            grow_array(aux.jobs, list_cap, need_list, -1, stream);
+            grow_array(aux.job_link, list_cap, need_list, -1, stream);
+            grow_array(aux.job_count, list_cap, need_list, 0, stream);
+            grow_array(aux.job_off, list_cap, need_list, 0, stream);
+            grow_array(aux.job_fill, list_cap, need_list, 0, stream);
+            list_cap = need_list;
+        }
+    }
+
+    // Room for a build of `pts` points in `jobs` jobs on top of the current pools.
+    void reserve_build(long long pts, long long jobs) {
+        long long min_leaf = std::max(1, (fill + 1) / 2);
+        long long leaves = pts / min_leaf + jobs + 2;
+        long long nodes = leaves + 2;
+        long long free_l = (long long)st->free_leaf_n + dt.leaf_cap - st->leaf_top;
+        long long free_n = (long long)st->free_node_n + dt.node_cap - st->node_top;
+        long long want_l = dt.leaf_cap, want_n = dt.node_cap;
+        if (free_l < leaves) want_l = (long long)st->leaf_top + leaves + leaves / 4 + 64;
+        if (free_n < nodes) want_n = (long long)st->node_top + nodes + nodes / 4 + 64;
+        ensure_pools(want_n, want_l);
+    }
+
+    void ensure_removed(long long need) {
+        if (need <= removed_cap) return;
+        long long nc = std::max(need, removed_cap * 3 / 2 + 1024);
+        grow_array(removed, (size_t)std::min<long long>(removed_cap, st->removed_n), (size_t)nc, -1, stream);
+        removed_cap = nc;
+    }
+
+    // ---- status ------------------------------------------------------------------
+    void read_status() {
+        CK(cudaMemcpyAsync(st, st_dev, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (st->err & ERR_POOL) throw Internal{"device pool exhausted"};
+        if (st->err & ERR_LOOP) throw Internal{"device loop cap reached (corrupted tree)"};
+    }
+    void zero_fields(size_t off, size_t bytes) {
+        CK(cudaMemsetAsync((char*)st_dev + off, 0, bytes, stream));
+    }
+    // Clears the per-call counters (everything but the pool state and removed_n).
+    void reset_counters() {
+        zero_fields(offsetof(DevStatus, err), offsetof(DevStatus, root_code) - offsetof(DevStatus, err));
+        zero_fields(offsetof(DevStatus, count), 2 * sizeof(long long));
+        zero_fields(offsetof(DevStatus, job_total), sizeof(long long));
+    }
+    void set_status_ll(size_t off, long long v) {
+        CK(cudaMemcpyAsync((char*)st_dev + off, &v, sizeof(v), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));  // v lives on this stack frame
+    }
+
+    // Empty tree: pools cleared, sentinel with no children.
+    void reset_tree() {
+        zero_fields(0, 6 * sizeof(int));
+        int one = 1;
+        CK(cudaMemcpyAsync(&st_dev->node_top, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
+        const float inf = INFINITY;
+        float rec[16] = {inf, inf, inf, -inf, -inf, -inf, inf, inf, inf, -inf, -inf, -inf, 0.f, 0.f, 0.f, 0.f};
+        int zero_codes[4] = {0, 0, 0, 0};
+        std::memcpy(&rec[12], zero_codes, sizeof(zero_codes));
+        int4 zc = make_int4(0, 0, 0, 0);
+        int minus1 = -1, h0 = 0;
+        CK(cudaMemcpyAsync(dt.node, rec, sizeof(rec), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(dt.ncnt, &zc, sizeof(zc), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(dt.nparent, &minus1, sizeof(int), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(dt.nheight, &h0, sizeof(int), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));  // the sources above live on this stack frame
+        st->node_top = 1;
+        st->leaf_top = 0;
+        st->free_node_n = st->free_leaf_n = 0;
+        st->root_code = 0;
+        st->root_slots = st->root_deleted = 0;
+    }
+
+    // ---- rebuild jobs ---------------------------------------------------------------
+    Criteria criteria() const { return Criteria{del_param, bal_param, min_size, fill}; }
+
+    // Runs the jobs selected in aux (st->n_jobs on the device, nj here):
+    // gather their valid points (plus overflow points), rebuild, relink and
+    // refit their ancestors.
+    void run_jobs(int nj, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+        small.ensure(scan_temp_bytes(nj + 1) + 1024, stream);
+        launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, nj, small.p, stream);
+        read_status();
+        long long total = st->job_total;
+        long long max_job = st->max_job;
+        reserve_build(total, nj);
+        ensure_removed(st->removed_n + st->root_deleted + 1);
+        size_t bytes = align_up(sizeof(float4) * std::max<long long>(total, 1)) +
+                       build_scratch_bytes(std::max<long long>(total, 1), nj, fill) + 4096;
+        bld.ensure(bytes, stream);
+        float4* gathered = (float4*)bld.p;
+        BuildScratch bs;
+        carve_build_scratch((char*)bld.p + align_up(sizeof(float4) * std::max<long long>(total, 1)),
+                            std::max<long long>(total, 1), nj, fill, &bs);
+        launch_job_gather(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_pts, ovf_bound, gathered, removed,
+                          removed_cap, stream);
+        build_subtrees(dt, gathered, total, aux.job_off, aux.job_link, nj, std::max<long long>(max_job, 1), fill, bs,
+                       stream);
+        zero_fields(offsetof(DevStatus, n_items), sizeof(int));
+        zero_fields(offsetof(DevStatus, n_viol), sizeof(int));
+        launch_job_finish(dt, aux, nj, stream);
+        zero_fields(offsetof(DevStatus, n_jobs), sizeof(int));
+        launch_refit(dt, aux, aux.items, &st_dev->n_items, nj, criteria(), stream);
+    }
+
+    // After a mutation queued dirty leaves in aux.items: refit, then rebuild
+    // the topmost subtrees that violate the criteria (up to three rounds).
+    void finish_update(const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+        int bound = st->leaf_top + st->node_top + 1;
+        launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
+        launch_clear_dirty(dt, aux, bound, stream);
+        // Rebuilding a subtree can unbalance its ancestors; each round moves
+        // the violations up, so a few rounds settle the tree.
+        for (int round = 0; round < 8; ++round) {
+            read_status();
+            int nv = st->n_viol;
+            if (nv == 0) break;
+            if (round == 7) {
+                // Still unsettled: clear the flags; the next call retries.
+                launch_clear_viol(dt, aux, nv, stream);
+                break;
+            }
+            launch_select_jobs(dt, aux, nv, stream);
+            read_status();
+            int nj = st->n_jobs;
+            if (nj == 0) throw Internal{"violators without a topmost job"};
+            run_jobs(nj, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
+            zero_fields(offsetof(DevStatus, n_items), sizeof(int));
+        }
+        zero_fields(offsetof(DevStatus, n_viol), sizeof(int));
+        launch_snapshot_root(dt, stream);
+        read_status();
+        if (st->err & ERR_STACK) throw Internal{"tree deeper than the traversal stack"};
+        if (st->err & ERR_ID) throw CapacityFail{"point id space exhausted"};
+    }
+
+    // Builds the points `pts` (device, {x,y,z,id}) as the whole tree.
+    void build_root(const float4* pts, long long n) {
+        long long nn = std::max<long long>(n, 1);
+        reserve_build(n, 1);
+        int host_job[3] = {0, (int)n, 0};
+        small.ensure(4096, stream);
+        int* job = (int*)small.p;
+        CK(cudaMemcpyAsync(job, host_job, sizeof(host_job), cudaMemcpyHostToDevice, stream));
+        bld.ensure(build_scratch_bytes(nn, 1, fill) + 4096, stream);
+        BuildScratch bs;
+        carve_build_scratch(bld.p, nn, 1, fill, &bs);
+        build_subtrees(dt, pts, n, job, job + 2, 1, nn, fill, bs, stream);
+        launch_snapshot_root(dt, stream);
+        read_status();
+    }
+
+    // ---- API -----------------------------------------------------------------------
+    void build(const float* xyz, long long n, int stride) {
+        if (n < 0 || stride < 3 || (n > 0 && xyz == nullptr)) throw BadArg{"build: bad arguments"};
+        if (n > MAX_ID) throw CapacityFail{"build: too many points"};
+        reset_counters();
+        float4* packed = nullptr;
+        if (n > 0) {
+            op.ensure(align_up(sizeof(float) * n * stride) + align_up(sizeof(float4) * n), stream);
+            Carver c(op.p);
+            float* raw = c.take<float>((size_t)n * stride);
+            packed = c.take<float4>(n);
+            CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
+            launch_pack_points(dt, raw, stride, n, 0, packed, stream);
+            read_status();
+            if (st->err & ERR_INPUT) throw BadArg{"build: non-finite coordinate"};
+        }
+        reset_tree();
+        next_id = n;
+        if (n == 0) {
+            launch_snapshot_root(dt, stream);
+            read_status();
+            return;
+        }
+        build_root(packed, n);
+    }
+
+    void add_points(const float* xyz, long long n, int stride, bool downsample, long long* n_added) {
+        if (n < 0 || stride < 3 || (n > 0 && xyz == nullptr)) throw BadArg{"add_points: bad arguments"};
+        if (n_added) *n_added = 0;
+        if (n == 0) return;
+        if (next_id + n > (long long)MAX_ID + 1) throw CapacityFail{"point id space exhausted"};
+        if (downsample && !(ds_size > 0.f && std::isfinite(ds_size))) throw BadArg{"downsample size must be > 0"};
+        reset_counters();
+        if (!downsample) {
+            op.ensure(align_up(sizeof(float) * n * stride) + 2 * align_up(sizeof(float4) * n) +
+                          align_up(sizeof(int4) * n),
+                      stream);
+            Carver c(op.p);
+            float* raw = c.take<float>((size_t)n * stride);
+            float4* packed = c.take<float4>(n);
+            int4* ovf_leaf = c.take<int4>(n);
+            float4* ovf_pts = c.take<float4>(n);
+            CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
+            launch_pack_points(dt, raw, stride, n, next_id, packed, stream);
+            read_status();
+            if (st->err & ERR_INPUT) throw BadArg{"add_points: non-finite coordinate"};
+            next_id += n;
+            if (st->root_code == 0) {
+                build_root(packed, n);
+                return;
+            }
+            launch_route_append(dt, aux, packed, n, ovf_leaf, ovf_pts, stream);
+            finish_update(ovf_leaf, ovf_pts, (int)n);
+            return;
+        }
+        // Voxel downsampling.
+        op.ensure(align_up(sizeof(float) * n * stride) + ds_scratch_bytes(n) + align_up(sizeof(float4) * n) +
+                      align_up(sizeof(int4) * n) + 4096,
+                  stream);
+        Carver c(op.p);
+        float* raw = c.take<float>((size_t)n * stride);
+        int4* ovf_leaf = c.take<int4>(n);
+        float4* ovf_pts = c.take<float4>(n);
+        DsScratch d;
+        carve_ds_scratch(op.p == nullptr ? nullptr : (char*)op.p + c.off, n, &d);
+        CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
+        launch_ds_prepare(dt, raw, stride, n, ds_size, d, stream);
+        read_status();
+        if (st->err & ERR_INPUT) throw BadArg{"add_points: non-finite coordinate"};
+        const int n_groups = st->n_groups;
+        const long long first_id = next_id;
+        long long a = 0;
+        while (a < n) {
+            set_status_ll(offsetof(DevStatus, count), n);
+            launch_ds_search(dt, n, ds_size, a, d, n_groups, stream);
+            read_status();
+            long long e = std::min<long long>(std::max<long long>(st->count, a + 1), n);
+            zero_fields(offsetof(DevStatus, n_ins), sizeof(int));
+            launch_ds_fold(dt, aux, n, a, e, first_id, d, n_groups, stream);
+            if (st->root_code == 0) {
+                read_status();
+                if (st->n_ins > 0) build_root(d.ins, st->n_ins);
+            } else {
+                launch_route_append_dev_count(dt, aux, d.ins, n_groups, &st_dev->n_ins, ovf_leaf, ovf_pts, stream);
+                finish_update(ovf_leaf, ovf_pts, n_groups);
+            }
+            a = e;
+        }
+        next_id += n;
+        read_status();
+        if (n_added) *n_added = st->count2;
+    }
+
+    void delete_points(const float* xyz, long long n, int stride) {
+        if (n < 0 || stride < 3 || (n > 0 && xyz == nullptr)) throw BadArg{"delete_points: bad arguments"};
+        if (n == 0 || st->root_code == 0) return;
+        reset_counters();
+        op.ensure(align_up(sizeof(float) * n * stride), stream);
+        float* raw = (float*)op.p;
+        CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
+        launch_delete_points(dt, aux, raw, stride, n, stream);
+        finish_update(nullptr, nullptr, 0);
+    }
+
+    long long delete_boxes(const float* boxes, long long m) {
+        if (m < 0 || (m > 0 && boxes == nullptr)) throw BadArg{"delete_boxes: bad arguments"};
+        if (m == 0 || st->root_code == 0) return 0;
+        reset_counters();
+        op.ensure(align_up(sizeof(float) * m * 6), stream);
+        float* raw = (float*)op.p;
+        CK(cudaMemcpyAsync(raw, boxes, sizeof(float) * m * 6, cudaMemcpyHostToDevice, stream));
+        launch_delete_boxes(dt, aux, raw, m, F_DEL, (long long*)((char*)st_dev + offsetof(DevStatus, count)),
+                            stream);
+        read_status();
+        long long deleted = st->count;
+        finish_update(nullptr, nullptr, 0);
+        return deleted;
+    }
+
+    void add_boxes(const float* boxes, long long m) {
+        if (m < 0 || (m > 0 && boxes == nullptr)) throw BadArg{"add_boxes: bad arguments"};
+        if (m == 0 || st->root_code == 0) return;
+        reset_counters();
+        op.ensure(align_up(sizeof(float) * m * 6), stream);
+        float* raw = (float*)op.p;
+        CK(cudaMemcpyAsync(raw, boxes, sizeof(float) * m * 6, cudaMemcpyHostToDevice, stream));
+        launch_add_boxes(dt, aux, raw, m, stream);
+        finish_update(nullptr, nullptr, 0);
+    }
+
+    void knn(const float* q, long long nq, int stride, int k, double max_dist, int* ids, float* d2, float* xyz,
+             int* cnt, bool device_ptrs) {
+        if (nq < 0 || stride < 3 || k < 1 || (nq > 0 && (q == nullptr || ids == nullptr || d2 == nullptr)))
+            throw BadArg{"knn: bad arguments"};
+        if (nq == 0) return;
+        if ((long long)nq * k > (1ll << 31)) throw BadArg{"knn: nq * k too large"};
+        float lim = max_sq_threshold(max_dist);
+        size_t nk = (size_t)nq * k;
+        if (device_ptrs) {
+            int* slots = nullptr;
+            if (k > KNN_REG_MAX) {
+                small.ensure(align_up(sizeof(int) * nk), stream);
+                slots = (int*)small.p;
+            }
+            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, slots, stream);
+            CK(cudaGetLastError());
+            return;
+        }
+        reset_counters();
+        op.ensure(align_up(sizeof(float) * nq * stride) + align_up(sizeof(int) * nk) + align_up(sizeof(float) * nk) +
+                      align_up(sizeof(float) * nk * 3) + align_up(sizeof(int) * nq) + align_up(sizeof(int) * nk),
+                  stream);
+        Carver c(op.p);
+        float* dq = c.take<float>((size_t)nq * stride);
+        int* dids = c.take<int>(nk);
+        float* dd2 = c.take<float>(nk);
+        float* dxyz = xyz ? c.take<float>(nk * 3) : nullptr;
+        int* dcnt = cnt ? c.take<int>(nq) : nullptr;
+        int* slots = k > KNN_REG_MAX ? c.take<int>(nk) : nullptr;
+        CK(cudaMemcpyAsync(dq, q, sizeof(float) * nq * stride, cudaMemcpyHostToDevice, stream));
+        launch_knn(dt, dq, stride, nq, k, lim, dids, dd2, dxyz, dcnt, slots, stream);
+        CK(cudaMemcpyAsync(ids, dids, sizeof(int) * nk, cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(d2, dd2, sizeof(float) * nk, cudaMemcpyDeviceToHost, stream));
+        if (xyz) CK(cudaMemcpyAsync(xyz, dxyz, sizeof(float) * nk * 3, cudaMemcpyDeviceToHost, stream));
+        if (cnt) CK(cudaMemcpyAsync(cnt, dcnt, sizeof(int) * nq, cudaMemcpyDeviceToHost, stream));
+        read_status();
+        if (st->err & ERR_STACK) throw Internal{"knn: traversal stack overflow"};
+    }
+
+    // mode 0: boxes (6 floats each), mode 1: centres + radii.
+    void range(int mode, const float* q, long long nq, int stride, const float* radius, int rstride,
+               long long* offsets, int* ids, float* xyz, long long capacity, long long* total) {
+        if (nq < 0 || offsets == nullptr || total == nullptr || (nq > 0 && q == nullptr))
+            throw BadArg{"range search: bad arguments"};
+        if (mode == 1 && (stride < 3 || (nq > 0 && radius == nullptr) || rstride < 0))
+            throw BadArg{"radius search: bad arguments"};
+        int qs = mode == 0 ? 6 : stride;
+        *total = 0;
+        offsets[0] = 0;
+        if (nq == 0) return;
+        reset_counters();
+        op.ensure(align_up(sizeof(float) * nq * qs) + align_up(sizeof(float) * nq) +
+                      2 * align_up(sizeof(long long) * (nq + 1)),
+                  stream);
+        Carver c(op.p);
+        float* dq = c.take<float>((size_t)nq * qs);
+        float* dr = c.take<float>(nq);
+        long long* dcounts = c.take<long long>(nq + 1);
+        long long* doffs = c.take<long long>(nq + 1);
+        CK(cudaMemcpyAsync(dq, q, sizeof(float) * nq * qs, cudaMemcpyHostToDevice, stream));
+        std::vector<float> rr;
+        if (mode == 1) {
+            rr.resize(nq);
+            for (long long i = 0; i < nq; ++i) rr[i] = radius[i * rstride];
+            CK(cudaMemcpyAsync(dr, rr.data(), sizeof(float) * nq, cudaMemcpyHostToDevice, stream));
+        }
+        launch_range(dt, mode, dq, qs, dr, nq, dcounts, nullptr, nullptr, nullptr, stream);
+        std::vector<long long> counts(nq);
+        CK(cudaMemcpyAsync(counts.data(), dcounts, sizeof(long long) * nq, cudaMemcpyDeviceToHost, stream));
+        read_status();
+        if (st->err & ERR_STACK) throw Internal{"range search: traversal stack overflow"};
+        long long acc = 0;
+        for (long long i = 0; i < nq; ++i) {
+            offsets[i] = acc;
+            acc += counts[i];
+        }
+        offsets[nq] = acc;
+        *total = acc;
+        if (acc > capacity || (acc > 0 && ids == nullptr)) throw CapacityFail{"range search: output too small"};
+        if (acc == 0) return;
+        bld.ensure(align_up(sizeof(int) * acc) + align_up(sizeof(float) * acc * 3), stream);
+        Carver o(bld.p);
+        int* dids = o.take<int>(acc);
+        float* dxyz = xyz ? o.take<float>(acc * 3) : nullptr;
+        CK(cudaMemcpyAsync(doffs, offsets, sizeof(long long) * nq, cudaMemcpyHostToDevice, stream));
+        launch_range(dt, mode, dq, qs, dr, nq, nullptr, doffs, dids, dxyz, stream);
+        CK(cudaMemcpyAsync(ids, dids, sizeof(int) * acc, cudaMemcpyDeviceToHost, stream));
+        if (xyz) CK(cudaMemcpyAsync(xyz, dxyz, sizeof(float) * acc * 3, cudaMemcpyDeviceToHost, stream));
+        read_status();
+    }
+
+    void flatten(float* xyz, int* ids, long long capacity, long long* n) {
+        if (n == nullptr) throw BadArg{"flatten: bad arguments"};
+        long long valid = (long long)st->root_slots - st->root_deleted;
+        *n = valid;
+        if (valid > capacity || (valid > 0 && xyz == nullptr && ids == nullptr))
+            throw CapacityFail{"flatten: output too small"};
+        if (valid == 0) return;
+        reset_counters();
+        op.ensure(align_up(sizeof(float4) * valid), stream);
+        float4* out = (float4*)op.p;
+        launch_flatten(dt, out, (long long*)((char*)st_dev + offsetof(DevStatus, count)), stream);
+        std::vector<float4> h(valid);
+        CK(cudaMemcpyAsync(h.data(), out, sizeof(float4) * valid, cudaMemcpyDeviceToHost, stream));
+        read_status();
+        if (st->count != valid) throw Internal{"flatten: valid count mismatch"};
+        for (long long i = 0; i < valid; ++i) {
+            if (xyz) {
+                xyz[3 * i] = h[i].x;
+                xyz[3 * i + 1] = h[i].y;
+                xyz[3 * i + 2] = h[i].z;
+            }
+            if (ids) {
+                uint32_t w;
+                std::memcpy(&w, &h[i].w, 4);
+                ids[i] = (int)(w & ID_MASK);
+            }
+        }
+    }
+
+    void acquire_removed(float* xyz, long long capacity, long long* n) {
+        if (n == nullptr) throw BadArg{"acquire_removed_points: bad arguments"};
+        read_status();
+        long long k = std::min<long long>(st->removed_n, removed_cap);
+        *n = k;
+        if (k > capacity || (k > 0 && xyz == nullptr)) throw CapacityFail{"acquire_removed_points: output too small"};
+        if (k > 0) {
+            std::vector<float4> h(k);
+            CK(cudaMemcpyAsync(h.data(), removed, sizeof(float4) * k, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (long long i = 0; i < k; ++i) {
+                xyz[3 * i] = h[i].x;
+                xyz[3 * i + 1] = h[i].y;
+                xyz[3 * i + 2] = h[i].z;
+            }
+        }
+        zero_fields(offsetof(DevStatus, removed_n), sizeof(long long));
+        read_status();
+    }
+
+    void rebuild_all() {
+        if (st->root_code == 0) return;
+        reset_counters();
+        launch_select_root_job(dt, aux, stream);
+        run_jobs(1, nullptr, nullptr, 0);
+        finish_update(nullptr, nullptr, 0);
+    }
+
+    void tree_range(float* box6) {
+        float rec[6];
+        CK(cudaMemcpyAsync(rec, dt.node, sizeof(rec), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        bool empty = st->root_code == 0 || !(rec[0] <= rec[3]);
+        for (int a = 0; a < 6; ++a) box6[a] = empty ? 0.f : rec[a];
+    }
+
+    void root_alpha(float* bal, float* del) {
+        int slots = st->root_slots;
+        float b = 0.5f, d = 0.f;
+        if (st->root_code > 0 && slots > 0) {
+            int4 c;
+            CK(cudaMemcpyAsync(&c, dt.ncnt + st->root_code, sizeof(c), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            float fb = (float)c.x / (float)slots;
+            b = fb >= 0.5f ? fb : 1.f - fb;
+        }
+        if (slots > 0) d = (float)st->root_deleted / (float)slots;
+        if (bal) *bal = b;
+        if (del) *del = d;
+    }
+};
+
+}  // namespace ikdg
+
+struct ikdg_tree {
+    ikdg::Tree t;
+};
+
+namespace {
+
+int fail(ikdg_tree* h, int code, const std::string& msg) {
+    if (h != nullptr) h->t.err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(ikdg_tree* h, F&& f) {
+    if (h == nullptr) return IKDG_BAD_ARG;
+    std::lock_guard<std::mutex> lock(h->t.mu);
+    try {
+        CK(cudaSetDevice(h->t.device));
+        f(h->t);
+        return IKDG_OK;
+    } catch (const ikdg::CudaFail& e) {
+        return fail(h, IKDG_CUDA_ERR, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+    } catch (const ikdg::BadArg& e) {
+        return fail(h, IKDG_BAD_ARG, e.what);
+    } catch (const ikdg::CapacityFail& e) {
+        return fail(h, IKDG_CAPACITY, e.what);
+    } catch (const ikdg::Internal& e) {
+        return fail(h, IKDG_INTERNAL, e.what);
+    } catch (const std::bad_alloc&) {
+        return fail(h, IKDG_INTERNAL, "host allocation failed");
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ikdg_status_string(int s) {
+    switch (s) {
+        case IKDG_OK: return "ok";
+        case IKDG_BAD_ARG: return "bad argument";
+        case IKDG_CAPACITY: return "output capacity too small";
+        case IKDG_DEVICE_TIMEOUT: return "device wait timed out";
+        case IKDG_CUDA_ERR: return "CUDA error";
+        case IKDG_NO_DEVICE: return "no CUDA device";
+        case IKDG_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+const char* ikdg_last_error(const ikdg_tree* t) { return t ? t->t.err.c_str() : "null tree"; }
+
+int ikdg_create(float delete_param, float balance_param, float box_length, int device, ikdg_tree** out) {
+    if (out == nullptr) return IKDG_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return IKDG_NO_DEVICE;
+    }
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return IKDG_NO_DEVICE;
+    if (device >= ndev) return IKDG_BAD_ARG;
+    ikdg_tree* h = new (std::nothrow) ikdg_tree;
+    if (h == nullptr) return IKDG_INTERNAL;
+    h->t.del_param = delete_param;
+    h->t.bal_param = balance_param;
+    h->t.ds_size = box_length;
+    try {
+        h->t.init(device);
+    } catch (const ikdg::CudaFail& e) {
+        h->t.destroy();
+        delete h;
+        return IKDG_CUDA_ERR;
+    } catch (...) {
+        h->t.destroy();
+        delete h;
+        return IKDG_INTERNAL;
+    }
+    *out = h;
+    return IKDG_OK;
+}
+
+int ikdg_destroy(ikdg_tree* h) {
+    if (h == nullptr) return IKDG_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lock(h->t.mu);
+        cudaSetDevice(h->t.device);
+        h->t.destroy();
+    }
+    delete h;
+    return IKDG_OK;
+}
+
+int ikdg_set_delete_criterion_param(ikdg_tree* h, float v) {
+    return guarded(h, [&](ikdg::Tree& t) { t.del_param = v; });
+}
+int ikdg_set_balance_criterion_param(ikdg_tree* h, float v) {
+    return guarded(h, [&](ikdg::Tree& t) { t.bal_param = v; });
+}
+int ikdg_set_downsample_param(ikdg_tree* h, float v) {
+    return guarded(h, [&](ikdg::Tree& t) { t.ds_size = v; });
+}
+int ikdg_set_leaf_fill(ikdg_tree* h, int fill) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (fill < 4 || fill > ikdg::LEAF_CAP) throw ikdg::BadArg{"leaf fill must be in [4, 32]"};
+        t.fill = fill;
+    });
+}
+
+int ikdg_build(ikdg_tree* h, const float* xyz, int64_t n, int32_t stride) {
+    return guarded(h, [&](ikdg::Tree& t) { t.build(xyz, n, stride); });
+}
+
+int ikdg_add_points(ikdg_tree* h, const float* xyz, int64_t n, int32_t stride, int downsample_on, int64_t* n_added) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long a = 0;
+        t.add_points(xyz, n, stride, downsample_on != 0, &a);
+        if (n_added) *n_added = a;
+    });
+}
+
+int ikdg_delete_points(ikdg_tree* h, const float* xyz, int64_t n, int32_t stride) {
+    return guarded(h, [&](ikdg::Tree& t) { t.delete_points(xyz, n, stride); });
+}
+
+int ikdg_delete_boxes(ikdg_tree* h, const float* boxes, int64_t m, int64_t* n_deleted) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long d = t.delete_boxes(boxes, m);
+        if (n_deleted) *n_deleted = d;
+    });
+}
+
+int ikdg_add_boxes(ikdg_tree* h, const float* boxes, int64_t m) {
+    return guarded(h, [&](ikdg::Tree& t) { t.add_boxes(boxes, m); });
+}
+
+int ikdg_knn(ikdg_tree* h, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist, int32_t* ids,
+             float* d2, float* xyz, int32_t* cnt) {
+    return guarded(h, [&](ikdg::Tree& t) { t.knn(q, nq, stride, k, max_dist, ids, d2, xyz, cnt, false); });
+}
+
+int ikdg_knn_device(ikdg_tree* h, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
+                    int32_t* ids, float* d2, float* xyz, int32_t* cnt) {
+    return guarded(h, [&](ikdg::Tree& t) { t.knn(q, nq, stride, k, max_dist, ids, d2, xyz, cnt, true); });
+}
+
+int ikdg_box_search(ikdg_tree* h, const float* boxes, int64_t nb, int64_t* offsets, int32_t* ids, float* xyz,
+                    int64_t capacity, int64_t* total) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long tot = 0;
+        try {
+            t.range(0, boxes, nb, 6, nullptr, 0, (long long*)offsets, ids, xyz, capacity, &tot);
+        } catch (...) {
+            if (total) *total = tot;
+            throw;
+        }
+        if (total) *total = tot;
+    });
+}
+
+int ikdg_radius_search(ikdg_tree* h, const float* centers, int64_t nq, int32_t stride, const float* radius,
+                       int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
+                       int64_t* total) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long tot = 0;
+        try {
+            t.range(1, centers, nq, stride, radius, radius_stride, (long long*)offsets, ids, xyz, capacity, &tot);
+        } catch (...) {
+            if (total) *total = tot;
+            throw;
+        }
+        if (total) *total = tot;
+    });
+}
+
+int ikdg_size(ikdg_tree* h, int64_t* out) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (out == nullptr) throw ikdg::BadArg{"size: null output"};
+        *out = t.st->root_slots;
+    });
+}
+
+int ikdg_validnum(ikdg_tree* h, int64_t* out) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (out == nullptr) throw ikdg::BadArg{"validnum: null output"};
+        *out = (int64_t)t.st->root_slots - t.st->root_deleted;
+    });
+}
+
+int ikdg_tree_range(ikdg_tree* h, float* box6) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (box6 == nullptr) throw ikdg::BadArg{"tree_range: null output"};
+        t.tree_range(box6);
+    });
+}
+
+int ikdg_root_alpha(ikdg_tree* h, float* alpha_bal, float* alpha_del) {
+    return guarded(h, [&](ikdg::Tree& t) { t.root_alpha(alpha_bal, alpha_del); });
+}
+
+int ikdg_flatten(ikdg_tree* h, float* xyz, int32_t* ids, int64_t capacity, int64_t* n) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long k = 0;
+        try {
+            t.flatten(xyz, ids, capacity, &k);
+        } catch (...) {
+            if (n) *n = k;
+            throw;
+        }
+        if (n) *n = k;
+    });
+}
+
+int ikdg_acquire_removed_points(ikdg_tree* h, float* xyz, int64_t capacity, int64_t* n) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long k = 0;
+        try {
+            t.acquire_removed(xyz, capacity, &k);
+        } catch (...) {
+            if (n) *n = k;
+            throw;
+        }
+        if (n) *n = k;
+    });
+}
+
+int ikdg_rebuild(ikdg_tree* h) {
+    return guarded(h, [&](ikdg::Tree& t) { t.rebuild_all(); });
+}
+
+int ikdg_get_stream(ikdg_tree* h, void** stream) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (stream == nullptr) throw ikdg::BadArg{"get_stream: null output"};
+        *stream = (void*)t.stream;
+    });
+}
+
+int ikdg_set_stream(ikdg_tree* h, void* stream) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        CK(cudaStreamSynchronize(t.stream));
+        if (t.own_stream) CK(cudaStreamDestroy(t.stream));
+        t.stream = (cudaStream_t)stream;
+        t.own_stream = false;
+    });
+}
+
+int ikdg_synchronize(ikdg_tree* h) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        CK(cudaStreamSynchronize(t.stream));
+        CK(cudaGetLastError());
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// Host-side launchers shared between the translation units of libikdg.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ikdg {
+
+// ---- scan.cu / sort.cu ------------------------------------------------------
+// Exclusive prefix sum of n int32 values; `total` (device, nullable) receives
+// the sum.  `temp` must hold scan_temp_bytes(n) bytes.
+size_t scan_temp_bytes(long long n);
+void exclusive_scan(const int* in, int* out, long long n, int* total, void* temp, cudaStream_t s);
+
+// Stable LSD radix sort of `batch` independent (key, value) arrays of length n
+// stored `stride` elements apart, on the low `bits` bits of the key (a
+// multiple of 8).  The result lands back in keys / vals; the *_alt buffers are
+// scratch of the same shape.  `temp` must hold sort_temp_bytes(n, batch).
+size_t sort_temp_bytes(long long n, int batch);
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, long long n,
+                      int batch, long long stride, int bits, void* temp, cudaStream_t s);
+
+// ---- build.cu ---------------------------------------------------------------
+// Batched subtree build.  `pts` holds the points of `njobs` jobs back to back
+// (job j = [job_off[j], job_off[j+1])), each as {x, y, z, id}.  Every job
+// becomes a balanced subtree of leaves holding at most `fill` points, split at
+// the median of the longest AABB axis, and is linked into the child slot
+// `job_link[j]` (= parent * 2 + side) together with its AABB and counts.
+struct BuildScratch {
+    uint32_t* ord[2];    // 2 x [3 * n] point indices sorted per axis
+    uint32_t* keys[2];   // 2 x [3 * n]
+    int* segpos[2];      // 2 x [n]
+    int* flag;           // [n]
+    int* scan_in;        // [3 * n]
+    int* scan_out;       // [3 * n]
+    int4* segs[2];       // 2 x [max_segs]  {s, e, link, pad}
+    int4* seginfo;       // [max_segs]      {kind, axis/leaf, mid, child_base}
+    int* nseg;           // [2] device counters
+    void* temp;          // scan / sort temp
+};
+size_t build_scratch_bytes(long long n, int njobs, int fill);
+void carve_build_scratch(void* base, long long n, int njobs, int fill, BuildScratch* bs);
+int build_levels(long long max_job, int fill);
+void build_subtrees(const DevTree& t, const float4* pts, long long n, const int* job_off, const int* job_link,
+                    int njobs, long long max_job, int fill, const BuildScratch& bs, cudaStream_t s);
+
+// ---- query.cu ---------------------------------------------------------------
+// k > 64 needs `slots`: k ints of device scratch per query (else nullptr).
+constexpr int KNN_REG_MAX = 64;
+void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq,
+                int* out_id, float* out_d2, float* out_xyz, int* out_cnt, int* slots, cudaStream_t s);
+// Box (mode 0) and radius (mode 1) search.  Pass 1 (ids == nullptr) writes
+// per-query hit counts into `counts`; pass 2 writes ids / xyz starting at
+// offsets[i].  Boxes are {min xyz, max xyz}; radius queries are {x, y, z} with
+// a per-query radius.
+void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius,
+                  long long nq, long long* counts, const long long* offsets, int* ids, float* xyz,
+                  cudaStream_t s);
+
+// ---- update.cu --------------------------------------------------------------
+struct UpdateScratch;
+}  // namespace ikdg

@@ -1,0 +1,1042 @@
+// Mutations of the device tree: point insertion, box / point deletion, box
+// re-insertion, bottom-up refit with the rebalancing criteria, rebuild-job
+// collection, and the exact voxel downsampling of Add_Points.
+//
+// Reference behaviour replaced here:
+//   Add_by_point (ikd-Tree/ikd_Tree.cpp:817-866): descend by `p[axis] < split`
+//     to a leaf bucket and append; a full bucket becomes a rebuild job.
+//   Delete_by_range / Delete_Point_Boxes (:535-556, :647-710): every valid
+//     point in the half-open box is flagged; the count of newly deleted points
+//     is returned.  Whole covered subtrees are flagged without box tests.
+//   Delete_by_point (:712-760): one valid point within EPSS = 1e-6 per axis is
+//     flagged per input point (same_point, :1368-1371).
+//   Add_by_range (:762-815): points deleted by box / point deletion (not by
+//     downsampling) inside the box are restored.
+//   Update / Criterion_Check / Rebuild (:1183-1323, :1089-1107, :624-645):
+//     counts and AABBs are refit bottom-up along the touched paths only; a
+//     node whose deleted share exceeds alpha_del or whose left share leaves
+//     [1 - alpha_bal, alpha_bal] is rebuilt, topmost first.
+#include <cuda_runtime.h>
+
+#include "update.cuh"
+
+namespace ikdg {
+namespace {
+
+inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+__device__ __forceinline__ float coord4(const float4& p, int a) { return a == 0 ? p.x : (a == 1 ? p.y : p.z); }
+
+__device__ __forceinline__ void mark_dirty(const UpdateAux& a, DevStatus* st, int L) {
+    if (atomicExch(&a.dirty_flag[L], 1) == 0) {
+        int i = atomicAdd(&st->n_items, 1);
+        a.items[i] = leaf_code(L);
+    }
+}
+
+// ---- insertion -----------------------------------------------------------------
+
+__global__ void route_append_kernel(DevTree t, UpdateAux a, const float4* __restrict__ pts, long long n,
+                                    const int* n_dev, int4* __restrict__ ovf_leaf, float4* __restrict__ ovf_pts) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long lim = n_dev != nullptr ? (long long)*n_dev : n;
+    if (i >= lim) return;
+    float4 p = pts[i];
+    int code = __float_as_int(t.node[3].x);  // sentinel's left child = root
+    if (code == 0) {
+        atomicOr(&t.st->err, ERR_POOL);
+        return;
+    }
+    int steps = 0;
+    while (code > 0) {
+        if (++steps > MAX_WALK) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            return;
+        }
+        float4 f3 = t.node[4 * code + 3];
+        int axis = __float_as_int(f3.w);
+        code = coord4(p, axis) < f3.z ? __float_as_int(f3.x) : __float_as_int(f3.y);
+    }
+    int L = code_leaf(code);
+    int slot = atomicAdd(&t.leaf_n[L], 1);
+    if (slot < LEAF_CAP) {
+        t.pts[(long long)L * LEAF_CAP + slot] = p;
+    } else {
+        int o = atomicAdd(&t.st->n_ovf, 1);
+        ovf_leaf[o] = make_int4(L, 0, 0, 0);
+        ovf_pts[o] = p;
+    }
+    mark_dirty(a, t.st, L);
+}
+
+// ---- refit -------------------------------------------------------------------
+
+__global__ void refit_mark_kernel(DevTree t, UpdateAux a, const int* __restrict__ items, const int* n_items) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_items) return;
+    int code = items[i];
+    int X;
+    if (code < 0) {
+        int lp = t.lparent[code_leaf(code)];
+        if (lp < 0) return;
+        X = lp >> 1;
+    } else {
+        X = code;
+    }
+    for (int steps = 0; X > 0; ++steps) {
+        if (steps > MAX_WALK) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            return;
+        }
+        if (atomicAdd(&a.pend[X], 1) > 0) break;
+        X = t.nparent[X] >> 1;
+    }
+}
+
+__device__ __forceinline__ int child_height(const DevTree& t, int code) {
+    return code > 0 ? __ldcg(&t.nheight[code]) : 0;
+}
+
+__device__ __forceinline__ int log2_ceil(int x) {
+    int r = 0;
+    while ((1 << r) < x && r < 30) ++r;
+    return r;
+}
+
+__global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restrict__ items, const int* n_items,
+                                     Criteria c, int fill) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_items) return;
+    int code = items[i];
+    int X;
+    if (code < 0) {
+        int L = code_leaf(code);
+        int lp = t.lparent[L];
+        if (lp < 0) return;
+        int n = __ldcg(&t.leaf_n[L]);
+        int m = n < LEAF_CAP ? n : LEAF_CAP;
+        Box3 b = empty_box();
+        int del = 0;
+        const float4* lpn = t.pts + (long long)L * LEAF_CAP;
+        for (int j = 0; j < m; ++j) {
+            float4 p = __ldcg(lpn + j);
+            if (__float_as_uint(p.w) & F_DEL)
+                ++del;
+            else
+                box_grow(b, p.x, p.y, p.z);
+        }
+        X = lp >> 1;
+        write_child_box(t.node, X, lp & 1, b);
+        write_child_cnt(t.ncnt, X, lp & 1, n, del);
+        if (n > LEAF_CAP) {  // an overflowing bucket must be split
+            int v = atomicAdd(&t.st->n_viol, 1);
+            a.viol[v] = code;
+        }
+    } else {
+        X = code;
+    }
+    for (int steps = 0; X > 0; ++steps) {
+        if (steps > MAX_WALK) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            return;
+        }
+        __threadfence();
+        int old = atomicAdd(&a.arrive[X], 1);
+        if (old + 1 < __ldcg(&a.pend[X])) return;
+        a.pend[X] = 0;
+        a.arrive[X] = 0;
+        NodeRec r = load_node_cg(t.node, X);
+        int4 cc = __ldcg(t.ncnt + X);
+        Box3 b = empty_box();
+        Box3 bl = r.box(0), br = r.box(1);
+        if (!box_empty(bl)) box_union(b, bl);
+        if (!box_empty(br)) box_union(b, br);
+        int slots = cc.x + cc.z, del = cc.y + cc.w;
+        int h = 1 + max(child_height(t, r.left()), child_height(t, r.right()));
+        t.nheight[X] = h;
+        bool viol = false;
+        if (slots > c.min_size) {
+            float fd = (float)del / (float)slots;
+            float fb = (float)cc.x / (float)slots;
+            viol = fd > c.alpha_del || fb > c.alpha_bal || fb < 1.0f - c.alpha_bal;
+        }
+        // Height guard: keeps every traversal stack within MAX_STACK.
+        int ideal = log2_ceil(slots / (fill > 0 ? fill : 1) + 1);
+        if (h > 2 * ideal + 8) viol = true;
+        if (viol) {
+            a.viol_flag[X] = 1;
+            int v = atomicAdd(&t.st->n_viol, 1);
+            a.viol[v] = X;
+        }
+        int lp = t.nparent[X];
+        int P = lp >> 1;
+        write_child_box(t.node, P, lp & 1, b);
+        write_child_cnt(t.ncnt, P, lp & 1, slots, del);
+        X = P;
+    }
+}
+
+__global__ void clear_dirty_kernel(UpdateAux a, const int* n_items) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_items) return;
+    int code = a.items[i];
+    if (code < 0) a.dirty_flag[code_leaf(code)] = 0;
+}
+
+// ---- rebuild jobs ----------------------------------------------------------------
+
+__global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_viol) return;
+    int code = a.viol[i];
+    int link = code < 0 ? t.lparent[code_leaf(code)] : t.nparent[code];
+    if (link < 0) return;
+    int X = link >> 1;
+    for (int steps = 0; X > 0; ++steps) {
+        if (steps > MAX_WALK) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            return;
+        }
+        if (a.viol_flag[X]) return;  // an ancestor is rebuilt instead
+        X = t.nparent[X] >> 1;
+    }
+    int j = atomicAdd(&t.st->n_jobs, 1);
+    a.jobs[j] = code;
+    a.job_link[j] = link;
+    if (code < 0)
+        a.job_of_leaf[code_leaf(code)] = j;
+    else
+        a.job_of_node[code] = j;
+}
+
+__global__ void clear_viol_kernel(UpdateAux a, const int* n_viol) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_viol) return;
+    int code = a.viol[i];
+    if (code > 0) a.viol_flag[code] = 0;
+}
+
+__device__ __forceinline__ int find_job_up(const DevTree& t, const UpdateAux& a, int X) {
+    for (int steps = 0; X > 0; ++steps) {
+        if (steps > MAX_WALK) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            return -1;
+        }
+        int j = a.job_of_node[X];
+        if (j >= 0) return j;
+        X = t.nparent[X] >> 1;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ int count_valid(const DevTree& t, int L) {
+    int n = t.leaf_n[L];
+    int m = n < LEAF_CAP ? n : LEAF_CAP;
+    int v = 0;
+    const float4* lp = t.pts + (long long)L * LEAF_CAP;
+    for (int j = 0; j < m; ++j) v += (__float_as_uint(lp[j].w) & F_DEL) ? 0 : 1;
+    return v;
+}
+
+__global__ void job_count_leaf_kernel(DevTree t, UpdateAux a, int leaf_top) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= leaf_top) return;
+    int lp = t.lparent[L];
+    if (lp < 0) {
+        a.leaf_job[L] = -1;
+        return;
+    }
+    int j = a.job_of_leaf[L];
+    if (j < 0) j = find_job_up(t, a, lp >> 1);
+    a.leaf_job[L] = j;
+    if (j >= 0) atomicAdd(&a.job_count[j], count_valid(t, L));
+}
+
+__global__ void job_count_node_kernel(DevTree t, UpdateAux a, int node_top) {
+    int X = blockIdx.x * blockDim.x + threadIdx.x;
+    if (X < 1 || X >= node_top) return;
+    if (t.nparent[X] < 0) {
+        a.node_job[X] = -1;
+        return;
+    }
+    a.node_job[X] = find_job_up(t, a, X);
+}
+
+__global__ void job_count_ovf_kernel(DevTree t, UpdateAux a, const int4* __restrict__ ovf_leaf, const int* n_ovf) {
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= *n_ovf) return;
+    int j = a.leaf_job[ovf_leaf[o].x];
+    if (j < 0) {
+        atomicOr(&t.st->err, ERR_POOL);
+        return;
+    }
+    atomicAdd(&a.job_count[j], 1);
+}
+
+__global__ void job_max_kernel(DevTree t, UpdateAux a, const int* n_jobs, const int* total) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) {
+        t.st->job_total = *total;
+        a.job_off[*n_jobs] = *total;
+    }
+    if (j >= *n_jobs) return;
+    atomicMax(&t.st->max_job, a.job_count[j]);
+}
+
+__global__ void job_gather_leaf_kernel(DevTree t, UpdateAux a, int leaf_top, float4* __restrict__ out,
+                                       float4* __restrict__ removed, long long removed_cap) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= leaf_top) return;
+    int j = a.leaf_job[L];
+    if (j < 0) return;
+    int n = t.leaf_n[L];
+    int m = n < LEAF_CAP ? n : LEAF_CAP;
+    const float4* lp = t.pts + (long long)L * LEAF_CAP;
+    int nv = count_valid(t, L);
+    int pos = a.job_off[j] + atomicAdd(&a.job_fill[j], nv);
+    for (int s = 0; s < m; ++s) {
+        float4 p = lp[s];
+        uint32_t w = __float_as_uint(p.w);
+        if (!(w & F_DEL)) {
+            out[pos++] = p;
+        } else if (!(w & F_DSDEL)) {
+            // Dropped deleted points are kept for acquire_removed_points
+            // (flatten with DELETE_POINTS_REC, ikd_Tree.cpp:1338-1342).
+            long long r = atomicAdd((unsigned long long*)&t.st->removed_n, 1ull);
+            if (r < removed_cap) removed[r] = make_float4(p.x, p.y, p.z, __uint_as_float(w & ID_MASK));
+        }
+    }
+    t.lparent[L] = -1;
+    t.leaf_n[L] = 0;
+    int f = atomicAdd(&t.st->free_leaf_n, 1);
+    t.free_leaf[f] = L;
+}
+
+__global__ void job_gather_node_kernel(DevTree t, UpdateAux a, int node_top) {
+    int X = blockIdx.x * blockDim.x + threadIdx.x;
+    if (X < 1 || X >= node_top) return;
+    if (a.node_job[X] < 0) return;
+    t.nparent[X] = -1;
+    int f = atomicAdd(&t.st->free_node_n, 1);
+    t.free_node[f] = X;
+}
+
+__global__ void job_gather_ovf_kernel(DevTree t, UpdateAux a, const int4* __restrict__ ovf_leaf,
+                                      const float4* __restrict__ ovf_pts, const int* n_ovf, float4* __restrict__ out) {
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= *n_ovf) return;
+    int j = a.leaf_job[ovf_leaf[o].x];
+    if (j < 0) return;
+    int pos = a.job_off[j] + atomicAdd(&a.job_fill[j], 1);
+    out[pos] = ovf_pts[o];
+}
+
+// Resets per-job state and queues each job's parent for the follow-up refit.
+__global__ void job_finish_kernel(DevTree t, UpdateAux a, const int* n_jobs) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) {
+        t.st->max_job = 0;
+        t.st->n_ovf = 0;
+    }
+    if (j >= *n_jobs) return;
+    int code = a.jobs[j];
+    if (code < 0)
+        a.job_of_leaf[code_leaf(code)] = -1;
+    else
+        a.job_of_node[code] = -1;
+    a.job_count[j] = 0;
+    a.job_fill[j] = 0;
+    int P = a.job_link[j] >> 1;
+    if (P > 0) {
+        int i = atomicAdd(&t.st->n_items, 1);
+        a.items[i] = P;
+    }
+}
+
+// ---- box / point deletion, box re-insertion ----------------------------------------
+
+constexpr int DB_THREADS = 128;
+constexpr int DB_STACK = DB_THREADS * (MAX_STACK + 2);
+
+// One CTA per box.  The CTA expands its share of the subtree cooperatively: each
+// round pops up to DB_THREADS items off a shared stack, and each thread either
+// expands a node (pushing the children that overlap the box, tagged when fully
+// covered) or processes a leaf.  MODE 0 deletes (flags |= del_flags), MODE 1
+// restores box-deleted points (Add_by_range).
+template <int MODE>
+__global__ void __launch_bounds__(DB_THREADS) box_edit_kernel(DevTree t, UpdateAux a, const float* __restrict__ boxes,
+                                                              long long m, uint32_t del_flags,
+                                                              long long* __restrict__ total) {
+    __shared__ int stack[DB_STACK];
+    __shared__ int top;
+    __shared__ long long block_cnt;
+    for (long long bi = blockIdx.x; bi < m; bi += gridDim.x) {
+        Box3 qb;
+        for (int k = 0; k < 3; ++k) {
+            qb.lo[k] = boxes[bi * 6 + k];
+            qb.hi[k] = boxes[bi * 6 + 3 + k];
+        }
+        if (threadIdx.x == 0) {
+            top = 0;
+            block_cnt = 0;
+            stack[top++] = 0 * 2;  // the sentinel record
+        }
+        __syncthreads();
+        long long my_cnt = 0;
+        for (int rounds = 0;; ++rounds) {
+            int cur_top = top;
+            if (cur_top == 0) break;
+            if (rounds > MAX_VISITS / DB_THREADS) {
+                if (threadIdx.x == 0) atomicOr(&t.st->err, ERR_LOOP);
+                break;
+            }
+            int n = cur_top < DB_THREADS ? cur_top : DB_THREADS;
+            int base = cur_top - n;
+            int item = threadIdx.x < n ? stack[base + threadIdx.x] : 0;
+            __syncthreads();
+            if (threadIdx.x == 0) top = base;
+            __syncthreads();
+            if (threadIdx.x < n) {
+                int code = item >> 1;  // arithmetic shift: floor(item / 2)
+                bool cov = item & 1;
+                if (code >= 0) {
+                    NodeRec r = load_node_cg(t.node, code);
+                    for (int side = 0; side < 2; ++side) {
+                        int c = side == 0 ? r.left() : r.right();
+                        if (c == 0) continue;
+                        Box3 b = r.box(side);
+                        bool ccov = cov;
+                        if (MODE == 0) {
+                            if (box_empty(b)) continue;
+                            if (!ccov) {
+                                if (qbox_disjoint(qb, b)) continue;
+                                ccov = qbox_covers(qb, b);
+                            }
+                        } else if (code > 0) {
+                            // AABBs bound valid points only; deleted points are
+                            // bounded by the split planes instead: the left
+                            // subtree holds coordinates <= split, the right >= split.
+                            int ax = r.axis();
+                            float sp = r.split();
+                            if (side == 0 && sp < qb.lo[ax]) continue;
+                            if (side == 1 && qb.hi[ax] <= sp) continue;
+                        }
+                        int pos = atomicAdd(&top, 1);
+                        if (pos < DB_STACK)
+                            stack[pos] = c * 2 + (ccov ? 1 : 0);
+                        else
+                            atomicOr(&t.st->err, ERR_STACK);
+                    }
+                } else {
+                    int L = code_leaf(code);
+                    int nl = t.leaf_n[L];
+                    int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
+                    float4* lp = t.pts + (long long)L * LEAF_CAP;
+                    bool any = false;
+                    for (int s = 0; s < ml; ++s) {
+                        float4 p = __ldcg(lp + s);
+                        uint32_t w = __float_as_uint(p.w);
+                        if (MODE == 0) {
+                            if (w & F_DEL) continue;
+                            if (!cov && !qbox_holds(qb, p.x, p.y, p.z)) continue;
+                            unsigned old = atomicOr((unsigned*)&lp[s].w, del_flags);
+                            if (!(old & F_DEL)) {
+                                ++my_cnt;
+                                any = true;
+                            }
+                        } else {
+                            if (!(w & F_DEL) || (w & F_DSDEL)) continue;
+                            if (!cov && !qbox_holds(qb, p.x, p.y, p.z)) continue;
+                            atomicAnd((unsigned*)&lp[s].w, ~F_DEL);
+                            any = true;
+                        }
+                    }
+                    if (any) mark_dirty(a, t.st, L);
+                }
+            }
+            __syncthreads();
+        }
+        if (MODE == 0 && my_cnt) atomicAdd((unsigned long long*)&block_cnt, (unsigned long long)my_cnt);
+        __syncthreads();
+        if (MODE == 0 && threadIdx.x == 0 && block_cnt) atomicAdd((unsigned long long*)total, (unsigned long long)block_cnt);
+        __syncthreads();
+    }
+}
+
+// same_point (ikd_Tree.cpp:1368-1371): |a - b| < 1e-6 per axis, the float
+// difference compared in double.
+__device__ __forceinline__ bool same_point(float ax, float ay, float az, float bx, float by, float bz) {
+    return (double)fabsf(__fsub_rn(ax, bx)) < 1e-6 && (double)fabsf(__fsub_rn(ay, by)) < 1e-6 &&
+           (double)fabsf(__fsub_rn(az, bz)) < 1e-6;
+}
+
+__global__ void __launch_bounds__(128) delete_points_kernel(DevTree t, UpdateAux a, const float* __restrict__ in,
+                                                            int stride, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float px = in[i * stride], py = in[i * stride + 1], pz = in[i * stride + 2];
+    // A match differs by < 1e-6 per axis; 2e-6 bounds the search box safely
+    // (a larger coordinate rounds p +- 2e-6 only where no match can exist).
+    Box3 sb;
+    sb.lo[0] = __fsub_rn(px, 2e-6f); sb.hi[0] = __fadd_rn(px, 2e-6f);
+    sb.lo[1] = __fsub_rn(py, 2e-6f); sb.hi[1] = __fadd_rn(py, 2e-6f);
+    sb.lo[2] = __fsub_rn(pz, 2e-6f); sb.hi[2] = __fadd_rn(pz, 2e-6f);
+    int stack[MAX_STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool start = true;
+    int visits = 0;
+    while (sp > 0) {
+        if (++visits > MAX_VISITS) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            break;
+        }
+        int code = stack[--sp];
+        if (start || code > 0) {
+            start = false;
+            NodeRec r = load_node_cg(t.node, code);
+            for (int side = 0; side < 2; ++side) {
+                int c = side == 0 ? r.left() : r.right();
+                if (c == 0) continue;
+                Box3 b = r.box(side);
+                if (box_empty(b)) continue;
+                bool far = false;
+                for (int k = 0; k < 3; ++k) far = far || b.lo[k] > sb.hi[k] || b.hi[k] < sb.lo[k];
+                if (far) continue;
+                if (sp < MAX_STACK)
+                    stack[sp++] = c;
+                else
+                    atomicOr(&t.st->err, ERR_STACK);
+            }
+        } else {
+            int L = code_leaf(code);
+            int nl = t.leaf_n[L];
+            int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
+            float4* lp = t.pts + (long long)L * LEAF_CAP;
+            for (int s = 0; s < ml; ++s) {
+                float4 p = __ldcg(lp + s);
+                unsigned w = __float_as_uint(p.w);
+                if (w & F_DEL) continue;
+                if (!same_point(p.x, p.y, p.z, px, py, pz)) continue;
+                unsigned old = atomicCAS((unsigned*)&lp[s].w, w, w | F_DEL);
+                if (old == w) {
+                    mark_dirty(a, t.st, L);
+                    return;
+                }
+            }
+        }
+    }
+}
+
+__global__ void flatten_kernel(DevTree t, float4* __restrict__ out, long long* counter) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= t.st->leaf_top) return;
+    if (t.lparent[L] < 0) return;
+    int n = t.leaf_n[L];
+    int m = n < LEAF_CAP ? n : LEAF_CAP;
+    const float4* lp = t.pts + (long long)L * LEAF_CAP;
+    int nv = count_valid(t, L);
+    if (nv == 0) return;
+    long long pos = (long long)atomicAdd((unsigned long long*)counter, (unsigned long long)nv);
+    for (int s = 0; s < m; ++s) {
+        float4 p = lp[s];
+        if (!(__float_as_uint(p.w) & F_DEL)) out[pos++] = p;
+    }
+}
+
+__global__ void select_root_job_kernel(DevTree t, UpdateAux a) {
+    int code = __float_as_int(t.node[3].x);
+    if (code == 0) return;
+    a.jobs[0] = code;
+    a.job_link[0] = 0;
+    if (code < 0)
+        a.job_of_leaf[code_leaf(code)] = 0;
+    else
+        a.job_of_node[code] = 0;
+    t.st->n_jobs = 1;
+}
+
+__global__ void snapshot_root_kernel(DevTree t) {
+    int4 c = t.ncnt[0];
+    t.st->root_code = __float_as_int(t.node[3].x);
+    t.st->root_slots = c.x;
+    t.st->root_deleted = c.y;
+    int rc = t.st->root_code;
+    t.st->root_height = rc > 0 ? t.nheight[rc] : 0;
+}
+
+// ---- voxel downsampling ------------------------------------------------------------
+//
+// Sequential semantics (Add_Points with downsample_on, ikd_Tree.cpp:422-449),
+// for new point p_i in order: box = the voxel of p_i, with
+// lo = floor(x / ds) * ds and hi = lo + ds in float, centre = lo + (hi - lo) / 2
+// in double rounded to float; S = valid points in the half-open box; the
+// winner is p_i unless a point of S is strictly closer to the centre; if
+// |S| > 1 or the winner is p_i (within EPSS), S is deleted (downsample flag)
+// and the winner is inserted as a new point.
+//
+// Parallel form: points are grouped by voxel.  A voxel's outcome depends only
+// on its own S and its own new points, taken in input order, as long as no
+// point lies in two voxel boxes or outside its own (float rounding can make the
+// boxes of neighbouring voxels overlap or leave gaps by one ulp).  Such points
+// are detected and processed alone, in input order, which keeps the result
+// identical to the sequential loop.  Among points of S at the same distance
+// the smaller id wins (the reference takes the first in traversal order).
+
+__device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ void voxel_axis(float c, float ds, float& f, float& lo, float& hi, float& mid) {
+    f = floorf(__fdiv_rn(c, ds));
+    lo = __fmul_rn(f, ds);
+    hi = __fadd_rn(lo, ds);
+    mid = __double2float_rn(__dadd_rn((double)lo, __dmul_rn((double)__fsub_rn(hi, lo), 0.5)));
+}
+
+// Is coordinate c inside the box range of voxel index f + df on this axis?
+__device__ __forceinline__ bool in_voxel_range(float c, float f, float df, float ds) {
+    float lo = __fmul_rn(__fadd_rn(f, df), ds);
+    float hi = __fadd_rn(lo, ds);
+    return lo <= c && c < hi;
+}
+
+__global__ void ds_prepare_kernel(DevTree t, const float* __restrict__ in, int stride, long long n, float ds,
+                                  DsScratch d) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float c[3] = {in[i * stride], in[i * stride + 1], in[i * stride + 2]};
+    if (!(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]))) atomicOr(&t.st->err, ERR_INPUT);
+    float f[3], lo[3], hi[3], mid[3];
+    bool clean = true;
+    for (int a = 0; a < 3; ++a) {
+        voxel_axis(c[a], ds, f[a], lo[a], hi[a], mid[a]);
+        clean = clean && lo[a] <= c[a] && c[a] < hi[a];
+        if (!(fabsf(f[a]) < 8388608.0f)) clean = false;  // f +- 1 must stay exact
+    }
+    if (clean)
+        for (int a = 0; a < 3; ++a)
+            if (in_voxel_range(c[a], f[a], -1.f, ds) || in_voxel_range(c[a], f[a], 1.f, ds)) clean = false;
+    d.pts[i] = make_float4(c[0], c[1], c[2], 0.f);
+    d.box_lo[i] = make_float4(lo[0], lo[1], lo[2], f[0]);
+    d.box_hi[i] = make_float4(hi[0], hi[1], hi[2], f[1]);
+    d.mid[i] = make_float4(mid[0], mid[1], mid[2], f[2]);
+    // Grouping key: the voxel's float indices (bit patterns), exact.
+    // -0.0 and +0.0 give the same box; adding +0.0 maps both to +0.0.
+    int kb[3];
+    for (int a = 0; a < 3; ++a) kb[a] = __float_as_int(__fadd_rn(f[a], 0.0f));
+    d.key[i] = make_int4(kb[0], kb[1], kb[2], clean ? 1 : 0);
+    uint32_t h = (uint32_t)kb[0] * 73856093u ^ (uint32_t)kb[1] * 19349663u ^ (uint32_t)kb[2] * 83492791u;
+    d.hkey[0][i] = mix32(h);
+    d.hval[0][i] = (uint32_t)i;
+}
+
+__device__ __forceinline__ bool same_key(const int4& a, const int4& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+__global__ void ds_leaders_kernel(long long n, DsScratch d, DevStatus* st) {
+    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t h = d.hkey[0][j];
+    int4 k = d.key[d.hval[0][j]];
+    for (long long jj = j - 1; jj >= 0 && d.hkey[0][jj] == h; --jj)
+        if (same_key(d.key[d.hval[0][jj]], k)) return;
+    int g = atomicAdd(&st->n_groups, 1);
+    d.groups[g] = (int)j;
+}
+
+// First member index >= a of group g (members are in increasing index order).
+__device__ __forceinline__ long long group_first_from(const DsScratch& d, long long n, int j, long long a) {
+    uint32_t h = d.hkey[0][j];
+    int4 k = d.key[d.hval[0][j]];
+    for (long long jj = j; jj < n && d.hkey[0][jj] == h; ++jj) {
+        uint32_t idx = d.hval[0][jj];
+        if (!same_key(d.key[idx], k)) continue;
+        if ((long long)idx >= a) return idx;
+    }
+    return -1;
+}
+
+__global__ void ds_h1_kernel(long long n, long long a, DsScratch d, DevStatus* st) {
+    long long i = a + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (d.key[i].w) return;
+    long long cut = i > a ? i : a + 1;
+    atomicMin((long long*)&st->count, cut);
+}
+
+__global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, long long a, DsScratch d, float ds) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= t.st->n_groups) return;
+    int j = d.groups[g];
+    long long first = group_first_from(d, n, j, a);
+    if (first < 0) {
+        d.g_info[g] = make_int4(0, -1, 0, 0);
+        return;
+    }
+    int lead = d.hval[0][j];
+    float4 blo = d.box_lo[lead], bhi = d.box_hi[lead], mid = d.mid[lead];
+    Box3 qb;
+    qb.lo[0] = blo.x; qb.lo[1] = blo.y; qb.lo[2] = blo.z;
+    qb.hi[0] = bhi.x; qb.hi[1] = bhi.y; qb.hi[2] = bhi.z;
+    const float fk[3] = {blo.w, bhi.w, mid.w};
+    int n0 = 0, best_slot = -1, best_id = 0x7fffffff;
+    float best_d = __int_as_float(0x7f800000);
+    float4 best_p = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool hazard = false;
+    int stack[MAX_STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool start = true;
+    int visits = 0;
+    while (sp > 0) {
+        if (++visits > MAX_VISITS) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            break;
+        }
+        int code = stack[--sp];
+        if (start || code > 0) {
+            start = false;
+            NodeRec r = load_node(t.node, code);
+            for (int side = 0; side < 2; ++side) {
+                int c = side == 0 ? r.left() : r.right();
+                if (c == 0) continue;
+                Box3 b = r.box(side);
+                if (box_empty(b) || qbox_disjoint(qb, b)) continue;
+                if (sp < MAX_STACK)
+                    stack[sp++] = c;
+                else
+                    atomicOr(&t.st->err, ERR_STACK);
+            }
+        } else {
+            int L = code_leaf(code);
+            int nl = t.leaf_n[L];
+            int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
+            const float4* lp = t.pts + (long long)L * LEAF_CAP;
+            for (int s = 0; s < ml; ++s) {
+                float4 p = __ldg(lp + s);
+                uint32_t w = __float_as_uint(p.w);
+                if (w & F_DEL) continue;
+                if (!qbox_holds(qb, p.x, p.y, p.z)) continue;
+                ++n0;
+                float dd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
+                int id = (int)(w & ID_MASK);
+                if (dd < best_d || (dd == best_d && id < best_id)) {
+                    best_d = dd;
+                    best_id = id;
+                    best_slot = L * LEAF_CAP + s;
+                    best_p = p;
+                }
+                const float pc[3] = {p.x, p.y, p.z};
+                for (int k = 0; k < 3; ++k)
+                    if (in_voxel_range(pc[k], fk[k], -1.f, ds) || in_voxel_range(pc[k], fk[k], 1.f, ds)) hazard = true;
+            }
+        }
+    }
+    d.g_info[g] = make_int4(n0, best_slot, best_id, hazard ? 1 : 0);
+    d.g_best[g] = make_float4(best_p.x, best_p.y, best_p.z, best_d);
+    if (hazard) {
+        long long cut = first > a ? first : a + 1;
+        atomicMin((long long*)&t.st->count, cut);
+    }
+}
+
+__global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, long long a, long long e,
+                                                      long long first_id, DsScratch d) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= t.st->n_groups) return;
+    int j = d.groups[g];
+    int4 info = d.g_info[g];
+    d.g_out[g] = make_int4(0, 0, 0, 0);
+    if (info.y == -1 && info.x == 0 && group_first_from(d, n, j, a) < 0) return;
+    uint32_t h = d.hkey[0][j];
+    int lead = d.hval[0][j];
+    int4 k = d.key[lead];
+    float4 mid = d.mid[lead];
+    float4 best = d.g_best[g];
+    const int n0 = info.x;
+    bool s_is_s0 = true, del_s0 = false, have_ins = false;
+    float cx = 0.f, cy = 0.f, cz = 0.f, cd = 0.f;
+    long long ins_idx = -1;
+    int triggers = 0;
+    for (long long jj = j; jj < n && d.hkey[0][jj] == h; ++jj) {
+        uint32_t idx = d.hval[0][jj];
+        if (!same_key(d.key[idx], k)) continue;
+        if ((long long)idx < a || (long long)idx >= e) continue;
+        float4 p = d.pts[idx];
+        float pd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
+        float wx = p.x, wy = p.y, wz = p.z, wd = pd;
+        bool trig;
+        if (s_is_s0) {
+            if (n0 > 0 && best.w < pd) {
+                wx = best.x; wy = best.y; wz = best.z; wd = best.w;
+            }
+            trig = n0 > 1 || same_point(p.x, p.y, p.z, wx, wy, wz);
+            if (trig) {
+                del_s0 = n0 > 0;
+                s_is_s0 = false;
+            }
+        } else {
+            if (cd < pd) {
+                wx = cx; wy = cy; wz = cz; wd = cd;
+            }
+            trig = same_point(p.x, p.y, p.z, wx, wy, wz);
+        }
+        if (trig) {
+            ++triggers;
+            cx = wx; cy = wy; cz = wz; cd = wd;
+            have_ins = true;
+            ins_idx = idx;
+        }
+    }
+    d.g_out[g] = make_int4(del_s0 ? 1 : 0, have_ins ? 1 : 0, triggers, 0);
+    if (triggers) atomicAdd((unsigned long long*)&t.st->count2, (unsigned long long)triggers);
+    if (have_ins) {
+        long long id = first_id + ins_idx;
+        if (id > MAX_ID) {
+            atomicOr(&t.st->err, ERR_ID);
+            return;
+        }
+        int q = atomicAdd(&t.st->n_ins, 1);
+        d.ins[q] = make_float4(cx, cy, cz, __int_as_float((int)id));
+    }
+}
+
+// Deletes (with the downsample flag) every valid point in the boxes of the
+// groups whose fold decided so.
+__global__ void __launch_bounds__(128) ds_delete_kernel(DevTree t, UpdateAux a, DsScratch d) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= t.st->n_groups) return;
+    if (!d.g_out[g].x) return;
+    int lead = d.hval[0][d.groups[g]];
+    float4 blo = d.box_lo[lead], bhi = d.box_hi[lead];
+    Box3 qb;
+    qb.lo[0] = blo.x; qb.lo[1] = blo.y; qb.lo[2] = blo.z;
+    qb.hi[0] = bhi.x; qb.hi[1] = bhi.y; qb.hi[2] = bhi.z;
+    int stack[MAX_STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    bool start = true;
+    int visits = 0;
+    while (sp > 0) {
+        if (++visits > MAX_VISITS) {
+            atomicOr(&t.st->err, ERR_LOOP);
+            break;
+        }
+        int code = stack[--sp];
+        if (start || code > 0) {
+            start = false;
+            NodeRec r = load_node(t.node, code);
+            for (int side = 0; side < 2; ++side) {
+                int c = side == 0 ? r.left() : r.right();
+                if (c == 0) continue;
+                Box3 b = r.box(side);
+                if (box_empty(b) || qbox_disjoint(qb, b)) continue;
+                if (sp < MAX_STACK)
+                    stack[sp++] = c;
+                else
+                    atomicOr(&t.st->err, ERR_STACK);
+            }
+        } else {
+            int L = code_leaf(code);
+            int nl = t.leaf_n[L];
+            int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
+            float4* lp = t.pts + (long long)L * LEAF_CAP;
+            bool any = false;
+            for (int s = 0; s < ml; ++s) {
+                float4 p = lp[s];
+                uint32_t w = __float_as_uint(p.w);
+                if (w & F_DEL) continue;
+                if (!qbox_holds(qb, p.x, p.y, p.z)) continue;
+                lp[s].w = __uint_as_float(w | F_DEL | F_DSDEL);
+                any = true;
+            }
+            if (any) mark_dirty(a, t.st, L);
+        }
+    }
+}
+
+__global__ void pack_points_kernel(DevTree t, const float* __restrict__ in, int stride, long long n, long long first_id,
+                                   float4* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float x = in[i * stride], y = in[i * stride + 1], z = in[i * stride + 2];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) atomicOr(&t.st->err, ERR_INPUT);
+    long long id = first_id + i;
+    if (id > MAX_ID) atomicOr(&t.st->err, ERR_ID);
+    out[i] = make_float4(x, y, z, __int_as_float((int)(id & ID_MASK)));
+}
+
+__global__ void check_finite_kernel(DevTree t, const float* __restrict__ in, long long count) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    if (!isfinite(in[i])) atomicOr(&t.st->err, ERR_INPUT);
+}
+
+inline size_t au(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+void launch_route_append(const DevTree& t, const UpdateAux& a, const float4* pts, long long n, int4* ovf_leaf,
+                         float4* ovf_pts, cudaStream_t s) {
+    if (n <= 0) return;
+    route_append_kernel<<<blocks_for(n, 256), 256, 0, s>>>(t, a, pts, n, nullptr, ovf_leaf, ovf_pts);
+}
+
+void launch_route_append_dev_count(const DevTree& t, const UpdateAux& a, const float4* pts, long long n_bound,
+                                   const int* n_dev, int4* ovf_leaf, float4* ovf_pts, cudaStream_t s) {
+    if (n_bound <= 0) return;
+    route_append_kernel<<<blocks_for(n_bound, 256), 256, 0, s>>>(t, a, pts, n_bound, n_dev, ovf_leaf, ovf_pts);
+}
+
+void launch_refit(const DevTree& t, const UpdateAux& a, const int* items, const int* n_items, int max_items,
+                  const Criteria& c, cudaStream_t s) {
+    if (max_items <= 0) return;
+    refit_mark_kernel<<<blocks_for(max_items, 256), 256, 0, s>>>(t, a, items, n_items);
+    refit_compute_kernel<<<blocks_for(max_items, 128), 128, 0, s>>>(t, a, items, n_items, c, c.fill);
+}
+
+void launch_clear_dirty(const DevTree& t, const UpdateAux& a, int max_items, cudaStream_t s) {
+    if (max_items <= 0) return;
+    clear_dirty_kernel<<<blocks_for(max_items, 256), 256, 0, s>>>(a, &t.st->n_items);
+}
+
+void launch_select_jobs(const DevTree& t, const UpdateAux& a, int max_viol, cudaStream_t s) {
+    if (max_viol <= 0) return;
+    select_jobs_kernel<<<blocks_for(max_viol, 256), 256, 0, s>>>(t, a, &t.st->n_viol);
+    clear_viol_kernel<<<blocks_for(max_viol, 256), 256, 0, s>>>(a, &t.st->n_viol);
+}
+
+void launch_clear_viol(const DevTree& t, const UpdateAux& a, int max_viol, cudaStream_t s) {
+    if (max_viol <= 0) return;
+    clear_viol_kernel<<<blocks_for(max_viol, 256), 256, 0, s>>>(a, &t.st->n_viol);
+}
+
+void launch_job_count(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
+                      int max_ovf, int max_jobs, void* scan_temp, cudaStream_t s) {
+    if (leaf_top > 0) job_count_leaf_kernel<<<blocks_for(leaf_top, 256), 256, 0, s>>>(t, a, leaf_top);
+    if (node_top > 1) job_count_node_kernel<<<blocks_for(node_top, 256), 256, 0, s>>>(t, a, node_top);
+    if (max_ovf > 0) job_count_ovf_kernel<<<blocks_for(max_ovf, 256), 256, 0, s>>>(t, a, ovf_leaf, &t.st->n_ovf);
+    // job_off = exclusive scan of job_count over max_jobs entries (unused tail
+    // entries are zero); the total lands in job_count[max_jobs].
+    exclusive_scan(a.job_count, a.job_off, max_jobs, a.job_off + max_jobs, scan_temp, s);
+    job_max_kernel<<<blocks_for(max_jobs, 256), 256, 0, s>>>(t, a, &t.st->n_jobs, a.job_off + max_jobs);
+}
+
+void launch_job_gather(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
+                       const float4* ovf_pts, int max_ovf, float4* out, float4* removed, long long removed_cap,
+                       cudaStream_t s) {
+    if (leaf_top > 0)
+        job_gather_leaf_kernel<<<blocks_for(leaf_top, 256), 256, 0, s>>>(t, a, leaf_top, out, removed, removed_cap);
+    if (node_top > 1) job_gather_node_kernel<<<blocks_for(node_top, 256), 256, 0, s>>>(t, a, node_top);
+    if (max_ovf > 0)
+        job_gather_ovf_kernel<<<blocks_for(max_ovf, 256), 256, 0, s>>>(t, a, ovf_leaf, ovf_pts, &t.st->n_ovf, out);
+}
+
+void launch_job_finish(const DevTree& t, const UpdateAux& a, int max_jobs, cudaStream_t s) {
+    job_finish_kernel<<<blocks_for(max_jobs > 0 ? max_jobs : 1, 256), 256, 0, s>>>(t, a, &t.st->n_jobs);
+}
+
+void launch_delete_boxes(const DevTree& t, const UpdateAux& a, const float* boxes, long long m, uint32_t flags,
+                         long long* total, cudaStream_t s) {
+    if (m <= 0) return;
+    unsigned g = (unsigned)(m < 65535 ? m : 65535);
+    box_edit_kernel<0><<<g, DB_THREADS, 0, s>>>(t, a, boxes, m, flags, total);
+}
+
+void launch_add_boxes(const DevTree& t, const UpdateAux& a, const float* boxes, long long m, cudaStream_t s) {
+    if (m <= 0) return;
+    unsigned g = (unsigned)(m < 65535 ? m : 65535);
+    box_edit_kernel<1><<<g, DB_THREADS, 0, s>>>(t, a, boxes, m, 0u, nullptr);
+}
+
+void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts, int stride, long long n,
+                          cudaStream_t s) {
+    if (n <= 0) return;
+    delete_points_kernel<<<blocks_for(n, 128), 128, 0, s>>>(t, a, pts, stride, n);
+}
+
+void launch_snapshot_root(const DevTree& t, cudaStream_t s) { snapshot_root_kernel<<<1, 1, 0, s>>>(t); }
+
+void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s) {
+    if (t.leaf_cap <= 0) return;
+    flatten_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, out, counter);
+}
+
+void launch_select_root_job(const DevTree& t, const UpdateAux& a, cudaStream_t s) {
+    select_root_job_kernel<<<1, 1, 0, s>>>(t, a);
+}
+
+void launch_pack_points(const DevTree& t, const float* in, int stride, long long n, long long first_id, float4* out,
+                        cudaStream_t s) {
+    if (n <= 0) return;
+    pack_points_kernel<<<blocks_for(n, 256), 256, 0, s>>>(t, in, stride, n, first_id, out);
+}
+
+void launch_check_finite(const DevTree& t, const float* in, long long count, cudaStream_t s) {
+    if (count <= 0) return;
+    check_finite_kernel<<<blocks_for(count, 256), 256, 0, s>>>(t, in, count);
+}
+
+size_t ds_scratch_bytes(long long n) {
+    size_t b = 0;
+    b += 5 * au(sizeof(float4) * n);   // pts, box_lo, box_hi, mid, ins
+    b += au(sizeof(int4) * n);         // key
+    b += 4 * au(sizeof(uint32_t) * n); // hkey x2, hval x2
+    b += au(sizeof(int) * n);          // groups
+    b += 2 * au(sizeof(int4) * n);     // g_info, g_out
+    b += au(sizeof(float4) * n);       // g_best
+    b += au(sort_temp_bytes(n, 1));
+    return b;
+}
+
+void carve_ds_scratch(void* base, long long n, DsScratch* d) {
+    char* p = (char*)base;
+    auto take = [&](size_t bytes) {
+        void* r = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return r;
+    };
+    d->pts = (float4*)take(sizeof(float4) * n);
+    d->box_lo = (float4*)take(sizeof(float4) * n);
+    d->box_hi = (float4*)take(sizeof(float4) * n);
+    d->mid = (float4*)take(sizeof(float4) * n);
+    d->ins = (float4*)take(sizeof(float4) * n);
+    d->key = (int4*)take(sizeof(int4) * n);
+    d->hkey[0] = (uint32_t*)take(sizeof(uint32_t) * n);
+    d->hkey[1] = (uint32_t*)take(sizeof(uint32_t) * n);
+    d->hval[0] = (uint32_t*)take(sizeof(uint32_t) * n);
+    d->hval[1] = (uint32_t*)take(sizeof(uint32_t) * n);
+    d->groups = (int*)take(sizeof(int) * n);
+    d->g_info = (int4*)take(sizeof(int4) * n);
+    d->g_out = (int4*)take(sizeof(int4) * n);
+    d->g_best = (float4*)take(sizeof(float4) * n);
+    d->temp = (void*)p;
+}
+
+void launch_ds_prepare(const DevTree& t, const float* in, int stride, long long n, float ds, DsScratch& d,
+                       cudaStream_t s) {
+    if (n <= 0) return;
+    ds_prepare_kernel<<<blocks_for(n, 256), 256, 0, s>>>(t, in, stride, n, ds, d);
+    radix_sort_pairs(d.hkey[0], d.hval[0], d.hkey[1], d.hval[1], n, 1, n, 32, d.temp, s);
+    ds_leaders_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, d, t.st);
+}
+
+void launch_ds_search(const DevTree& t, long long n, float ds, long long a, DsScratch& d, int max_groups,
+                      cudaStream_t s) {
+    if (n - a > 0) ds_h1_kernel<<<blocks_for(n - a, 256), 256, 0, s>>>(n, a, d, t.st);
+    if (max_groups > 0) ds_search_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, d, ds);
+}
+
+void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long long a, long long e, long long first_id,
+                    DsScratch& d, int max_groups, cudaStream_t s) {
+    if (max_groups <= 0) return;
+    ds_fold_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, e, first_id, d);
+    ds_delete_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, aux, d);
+}
+
+}  // namespace ikdg

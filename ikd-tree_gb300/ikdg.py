@@ -1,0 +1,298 @@
+"""Python binding of libikdg (the GB300 incremental k-d tree) over its C ABI.
+
+``KDTree`` mirrors ``KD_TREE<PointType>`` (ikd-Tree/ikd_Tree.h:225-248): same
+method names, argument meaning and return values, plus batched forms of the
+searches (``knn``, ``box_search``, ``radius_search``) that take all queries of a
+step at once.  Every method runs CUDA kernels through libikdg.so; there is no
+CPU code path, and constructing a tree without the library or without a GPU
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libikdg.so")
+
+OK, BAD_ARG, CAPACITY, DEVICE_TIMEOUT, CUDA_ERR, NO_DEVICE, INTERNAL = 0, 2, 3, 4, 5, 6, 7
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_vp = C.c_void_p
+
+# Every entry point of include/ikdg.h with its ctypes signature.
+SIGNATURES = {
+    "ikdg_status_string": (C.c_char_p, [C.c_int]),
+    "ikdg_last_error": (C.c_char_p, [_vp]),
+    "ikdg_create": (C.c_int, [C.c_float, C.c_float, C.c_float, C.c_int, C.POINTER(_vp)]),
+    "ikdg_destroy": (C.c_int, [_vp]),
+    "ikdg_set_delete_criterion_param": (C.c_int, [_vp, C.c_float]),
+    "ikdg_set_balance_criterion_param": (C.c_int, [_vp, C.c_float]),
+    "ikdg_set_downsample_param": (C.c_int, [_vp, C.c_float]),
+    "ikdg_set_leaf_fill": (C.c_int, [_vp, C.c_int]),
+    "ikdg_build": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32]),
+    "ikdg_add_points": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, C.c_int, _lp]),
+    "ikdg_delete_points": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32]),
+    "ikdg_delete_boxes": (C.c_int, [_vp, _fp, C.c_int64, _lp]),
+    "ikdg_add_boxes": (C.c_int, [_vp, _fp, C.c_int64]),
+    "ikdg_knn": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _ip, _fp, _fp, _ip]),
+    "ikdg_knn_device": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _vp, _vp, _vp, _vp]),
+    "ikdg_box_search": (C.c_int, [_vp, _fp, C.c_int64, _lp, _ip, _fp, C.c_int64, _lp]),
+    "ikdg_radius_search": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, _fp, C.c_int32, _lp, _ip, _fp, C.c_int64,
+                                     _lp]),
+    "ikdg_size": (C.c_int, [_vp, _lp]),
+    "ikdg_validnum": (C.c_int, [_vp, _lp]),
+    "ikdg_tree_range": (C.c_int, [_vp, _fp]),
+    "ikdg_root_alpha": (C.c_int, [_vp, _fp, _fp]),
+    "ikdg_flatten": (C.c_int, [_vp, _fp, _ip, C.c_int64, _lp]),
+    "ikdg_acquire_removed_points": (C.c_int, [_vp, _fp, C.c_int64, _lp]),
+    "ikdg_rebuild": (C.c_int, [_vp]),
+    "ikdg_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "ikdg_set_stream": (C.c_int, [_vp, _vp]),
+    "ikdg_synchronize": (C.c_int, [_vp]),
+}
+
+_lib = None
+
+
+class IkdgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ikdg error {status}: {msg}")
+        self.status = status
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libikdg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with `python ikd-tree_gb300/build.py` (the GPU path has no fallback)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _f32(a, width: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    return a.reshape(-1, width)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_fp)
+
+
+class KDTree:
+    """KD_TREE<PointType> on the GPU (xyz points, float32)."""
+
+    def __init__(self, delete_param: float = 0.5, balance_param: float = 0.6, box_length: float = 0.2,
+                 device: int = -1):
+        self.lib = load()
+        h = _vp()
+        st = self.lib.ikdg_create(delete_param, balance_param, box_length, device, C.byref(h))
+        if st != OK:
+            raise IkdgError(st, self.lib.ikdg_status_string(st).decode())
+        self.h = h
+
+    # -- plumbing --------------------------------------------------------------
+    def _check(self, st: int, what: str):
+        if st != OK:
+            msg = self.lib.ikdg_last_error(self.h).decode() if self.h else ""
+            raise IkdgError(st, f"{what}: {self.lib.ikdg_status_string(st).decode()} ({msg})")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ikdg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- parameters (ikd_Tree.h:228-231) -----------------------------------------
+    def Set_delete_criterion_param(self, v: float):
+        self._check(self.lib.ikdg_set_delete_criterion_param(self.h, v), "Set_delete_criterion_param")
+
+    def Set_balance_criterion_param(self, v: float):
+        self._check(self.lib.ikdg_set_balance_criterion_param(self.h, v), "Set_balance_criterion_param")
+
+    def set_downsample_param(self, v: float):
+        self._check(self.lib.ikdg_set_downsample_param(self.h, v), "set_downsample_param")
+
+    def InitializeKDTree(self, delete_param=0.5, balance_param=0.7, box_length=0.2):
+        self.Set_delete_criterion_param(delete_param)
+        self.Set_balance_criterion_param(balance_param)
+        self.set_downsample_param(box_length)
+
+    def set_leaf_fill(self, fill: int):
+        self._check(self.lib.ikdg_set_leaf_fill(self.h, fill), "set_leaf_fill")
+
+    # -- mutations -------------------------------------------------------------
+    def Build(self, pts):
+        a = _f32(pts, 3)
+        self._check(self.lib.ikdg_build(self.h, _p(a), a.shape[0], 3), "Build")
+
+    def Add_Points(self, pts, downsample_on: bool) -> int:
+        a = _f32(pts, 3)
+        n = C.c_int64(0)
+        self._check(self.lib.ikdg_add_points(self.h, _p(a), a.shape[0], 3, int(bool(downsample_on)), C.byref(n)),
+                    "Add_Points")
+        return n.value
+
+    def Delete_Points(self, pts):
+        a = _f32(pts, 3)
+        self._check(self.lib.ikdg_delete_points(self.h, _p(a), a.shape[0], 3), "Delete_Points")
+
+    def Delete_Point_Boxes(self, boxes) -> int:
+        b = _f32(boxes, 6)
+        n = C.c_int64(0)
+        self._check(self.lib.ikdg_delete_boxes(self.h, _p(b), b.shape[0], C.byref(n)), "Delete_Point_Boxes")
+        return n.value
+
+    def Add_Point_Boxes(self, boxes):
+        b = _f32(boxes, 6)
+        self._check(self.lib.ikdg_add_boxes(self.h, _p(b), b.shape[0]), "Add_Point_Boxes")
+
+    def rebuild(self):
+        self._check(self.lib.ikdg_rebuild(self.h), "rebuild")
+
+    # -- searches --------------------------------------------------------------
+    def knn(self, q, k: int, max_dist: float = math.inf, want_xyz: bool = True):
+        """Batched Nearest_Search: (ids[nq,k], d2[nq,k], xyz[nq,k,3] or None, count[nq])."""
+        qa = _f32(q, 3)
+        nq = qa.shape[0]
+        ids = np.empty((nq, k), np.int32)
+        d2 = np.empty((nq, k), np.float32)
+        xyz = np.empty((nq, k, 3), np.float32) if want_xyz else None
+        cnt = np.empty(nq, np.int32)
+        self._check(self.lib.ikdg_knn(self.h, _p(qa), nq, 3, k, float(max_dist), ids.ctypes.data_as(_ip), _p(d2),
+                                      _p(xyz), cnt.ctypes.data_as(_ip)), "knn")
+        return ids, d2, xyz, cnt
+
+    def Nearest_Search(self, point, k: int, max_dist: float = math.inf):
+        """Single query, reference signature: returns (points[c,3], distances[c])."""
+        ids, d2, xyz, cnt = self.knn(np.asarray(point, np.float32).reshape(1, 3), k, max_dist)
+        c = int(cnt[0])
+        return xyz[0, :c].copy(), d2[0, :c].copy()
+
+    def _range(self, fn, args, nq):
+        offs = np.zeros(nq + 1, np.int64)
+        total = C.c_int64(0)
+        st = fn(*args(offs, None, None, 0, total))
+        if st not in (OK, CAPACITY):
+            self._check(st, "range search")
+        t = total.value
+        ids = np.empty(max(t, 1), np.int32)
+        xyz = np.empty((max(t, 1), 3), np.float32)
+        if t > 0:
+            self._check(fn(*args(offs, ids, xyz, t, total)), "range search")
+        return offs, ids[:t], xyz[:t]
+
+    def box_search(self, boxes):
+        """Batched Box_Search: (offsets[nb+1], ids[total], xyz[total,3])."""
+        b = _f32(boxes, 6)
+        nb = b.shape[0]
+
+        def args(offs, ids, xyz, cap, total):
+            return (self.h, _p(b), nb, offs.ctypes.data_as(_lp),
+                    None if ids is None else ids.ctypes.data_as(_ip), _p(xyz), cap, C.byref(total))
+        return self._range(self.lib.ikdg_box_search, args, nb)
+
+    def radius_search(self, q, radius):
+        """Batched Radius_Search: (offsets[nq+1], ids[total], xyz[total,3])."""
+        qa = _f32(q, 3)
+        nq = qa.shape[0]
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, np.float32), (nq,)))
+
+        def args(offs, ids, xyz, cap, total):
+            return (self.h, _p(qa), nq, 3, _p(r), 1, offs.ctypes.data_as(_lp),
+                    None if ids is None else ids.ctypes.data_as(_ip), _p(xyz), cap, C.byref(total))
+        return self._range(self.lib.ikdg_radius_search, args, nq)
+
+    def Box_Search(self, box):
+        offs, ids, xyz = self.box_search(np.asarray(box, np.float32).reshape(1, 6))
+        return xyz
+
+    def Radius_Search(self, point, radius: float):
+        offs, ids, xyz = self.radius_search(np.asarray(point, np.float32).reshape(1, 3), radius)
+        return xyz
+
+    # -- state -------------------------------------------------------------------
+    def size(self) -> int:
+        n = C.c_int64(0)
+        self._check(self.lib.ikdg_size(self.h, C.byref(n)), "size")
+        return n.value
+
+    def validnum(self) -> int:
+        n = C.c_int64(0)
+        self._check(self.lib.ikdg_validnum(self.h, C.byref(n)), "validnum")
+        return n.value
+
+    def tree_range(self) -> np.ndarray:
+        out = np.zeros(6, np.float32)
+        self._check(self.lib.ikdg_tree_range(self.h, _p(out)), "tree_range")
+        return out
+
+    def root_alpha(self):
+        b = C.c_float(0)
+        d = C.c_float(0)
+        self._check(self.lib.ikdg_root_alpha(self.h, C.byref(b), C.byref(d)), "root_alpha")
+        return b.value, d.value
+
+    def flatten(self, with_ids: bool = False):
+        n = C.c_int64(0)
+        st = self.lib.ikdg_flatten(self.h, None, None, 0, C.byref(n))
+        if st not in (OK, CAPACITY):
+            self._check(st, "flatten")
+        k = n.value
+        xyz = np.empty((max(k, 1), 3), np.float32)
+        ids = np.empty(max(k, 1), np.int32)
+        if k > 0:
+            self._check(self.lib.ikdg_flatten(self.h, _p(xyz), ids.ctypes.data_as(_ip), k, C.byref(n)), "flatten")
+        return (xyz[:k], ids[:k]) if with_ids else xyz[:k]
+
+    def acquire_removed_points(self) -> np.ndarray:
+        n = C.c_int64(0)
+        st = self.lib.ikdg_acquire_removed_points(self.h, None, 0, C.byref(n))
+        if st == OK and n.value == 0:
+            return np.zeros((0, 3), np.float32)
+        if st not in (OK, CAPACITY):
+            self._check(st, "acquire_removed_points")
+        k = n.value
+        xyz = np.empty((k, 3), np.float32)
+        self._check(self.lib.ikdg_acquire_removed_points(self.h, _p(xyz), k, C.byref(n)), "acquire_removed_points")
+        return xyz
+
+    # -- streams ---------------------------------------------------------------
+    def stream(self) -> int:
+        s = _vp()
+        self._check(self.lib.ikdg_get_stream(self.h, C.byref(s)), "get_stream")
+        return s.value or 0
+
+    def synchronize(self):
+        self._check(self.lib.ikdg_synchronize(self.h), "synchronize")
+
+    def knn_device(self, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int,
+                   xyz_ptr: int = 0, cnt_ptr: int = 0, stride: int = 3):
+        """kNN on device buffers (raw pointers), asynchronous on the tree's stream."""
+        self._check(self.lib.ikdg_knn_device(self.h, _vp(q_ptr), nq, stride, k, float(max_dist), _vp(ids_ptr),
+                                             _vp(d2_ptr), _vp(xyz_ptr or None), _vp(cnt_ptr or None)),
+                    "knn_device")

@@ -1,0 +1,150 @@
+/*
+ * ikdg.h - C ABI of the GB300 incremental k-d tree (libikdg.so).
+ *
+ * A drop-in replacement for the hot path of hku-mars/ikd-Tree's
+ * KD_TREE<PointType> (ikd-Tree/ikd_Tree.h:59-249): the tree lives in GPU memory
+ * and every call below runs CUDA kernels on one GPU.  There is no CPU fallback:
+ * without a usable CUDA device ikdg_create fails with IKDG_NO_DEVICE.
+ *
+ * Conventions
+ *   - Points are float xyz triples; `stride` is the distance in floats between
+ *     consecutive points (3 for packed xyz, 4 for pcl::PointXYZ, ...).
+ *   - Boxes are 6 floats {min x, min y, min z, max x, max y, max z}
+ *     (BoxPointType, ikd-Tree/ikd_Tree.h:32-35); box tests are half-open,
+ *     min <= p < max, as in the reference.
+ *   - Every point gets a 32-bit id when it enters the tree: Build numbers its
+ *     points 0..n-1, later insertions continue the sequence.  Searches report
+ *     ids; distance ties are broken by the smaller id.
+ *   - Functions taking host pointers are synchronous.  *_device variants take
+ *     device pointers and are asynchronous on the tree's stream.
+ *   - All functions return an ikdg_status code.
+ *
+ * Thread safety: calls on one tree are serialised by an internal mutex; the
+ * reference's concurrent Nearest_Search callers (ikd_Tree.cpp:875-884) are
+ * therefore safe, and mutations from several threads are ordered.
+ */
+#ifndef IKDG_H
+#define IKDG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ikdg_tree ikdg_tree;
+
+enum ikdg_status {
+    IKDG_OK = 0,
+    IKDG_BAD_ARG = 2,        /* invalid argument (null pointer, k <= 0, NaN / inf point ...) */
+    IKDG_CAPACITY = 3,       /* an output buffer is too small; the required size is reported */
+    IKDG_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up */
+    IKDG_CUDA_ERR = 5,       /* a CUDA runtime call failed; see ikdg_last_error */
+    IKDG_NO_DEVICE = 6,      /* no usable CUDA device */
+    IKDG_INTERNAL = 7        /* an internal invariant failed; see ikdg_last_error */
+};
+
+const char* ikdg_status_string(int status);
+/* Text of the last error on this tree (thread-unsafe across trees: per tree). */
+const char* ikdg_last_error(const ikdg_tree* t);
+
+/* KD_TREE(float delete_param, float balance_param, float box_length)
+ * (ikd-Tree/ikd_Tree.h:226, ikd_Tree.cpp:9-17).  `device` selects the CUDA
+ * device (-1: the current one). */
+int ikdg_create(float delete_param, float balance_param, float box_length, int device, ikdg_tree** out);
+/* ~KD_TREE (ikd_Tree.cpp:19-27). */
+int ikdg_destroy(ikdg_tree* t);
+
+/* Set_delete_criterion_param / Set_balance_criterion_param /
+ * set_downsample_param (ikd_Tree.h:228-230, ikd_Tree.cpp:29-42). */
+int ikdg_set_delete_criterion_param(ikdg_tree* t, float delete_param);
+int ikdg_set_balance_criterion_param(ikdg_tree* t, float balance_param);
+int ikdg_set_downsample_param(ikdg_tree* t, float box_length);
+/* Points per leaf bucket written by (re)builds, 4..32 (default 16). */
+int ikdg_set_leaf_fill(ikdg_tree* t, int fill);
+
+/* Build(PointVector) (ikd_Tree.h:235, ikd_Tree.cpp:352-364). */
+int ikdg_build(ikdg_tree* t, const float* xyz, int64_t n, int32_t stride);
+
+/* Add_Points(PointVector&, bool downsample_on) (ikd_Tree.h:239,
+ * ikd_Tree.cpp:413-489).  *n_added receives the reference's return value: the
+ * number of downsampling insertions, 0 without downsampling.  Unlike the
+ * reference (which dereferences a null root, ikd_Tree.cpp:472) adding to an
+ * empty tree works. */
+int ikdg_add_points(ikdg_tree* t, const float* xyz, int64_t n, int32_t stride, int downsample_on, int64_t* n_added);
+
+/* Delete_Points(PointVector&) (ikd_Tree.h:241, ikd_Tree.cpp:513-533): each
+ * input point deletes one valid point within 1e-6 per axis, if any. */
+int ikdg_delete_points(ikdg_tree* t, const float* xyz, int64_t n, int32_t stride);
+
+/* Delete_Point_Boxes(vector<BoxPointType>&) (ikd_Tree.h:242,
+ * ikd_Tree.cpp:535-556).  *n_deleted = number of valid points deleted. */
+int ikdg_delete_boxes(ikdg_tree* t, const float* boxes, int64_t m, int64_t* n_deleted);
+
+/* Add_Point_Boxes(vector<BoxPointType>&) (ikd_Tree.h:240,
+ * ikd_Tree.cpp:491-511): restores points inside the boxes that were deleted by
+ * box or point deletion and are still stored. */
+int ikdg_add_boxes(ikdg_tree* t, const float* boxes, int64_t m);
+
+/* Nearest_Search(point, k, Nearest_Points, Point_Distance, max_dist)
+ * (ikd_Tree.h:236, ikd_Tree.cpp:366-397), batched over nq queries.  Row i of
+ * the outputs holds the k nearest valid points whose float squared distance
+ * is <= max_dist * max_dist evaluated in double, as the reference does
+ * (ikd_Tree.cpp:872, :887; INFINITY: unbounded), ascending; missing
+ * entries have id -1 and distance +inf.  out_xyz (nq*k*3) and out_count (nq)
+ * may be NULL.  k >= 1 (k <= 64 keeps the candidates in registers). */
+int ikdg_knn(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
+             int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
+/* Same with device pointers; asynchronous on the tree's stream. */
+int ikdg_knn_device(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
+                    int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
+
+/* Box_Search(const BoxPointType&, PointVector&) (ikd_Tree.h:237,
+ * ikd_Tree.cpp:399-404), batched over nb boxes.  Results are CSR: hits of box
+ * i are ids[offsets[i] .. offsets[i+1]) (and xyz, 3 floats each, may be NULL).
+ * offsets has nb + 1 entries.  When *total exceeds `capacity`, nothing but
+ * offsets and *total is written and IKDG_CAPACITY is returned. */
+int ikdg_box_search(ikdg_tree* t, const float* boxes, int64_t nb, int64_t* offsets, int32_t* ids, float* xyz,
+                    int64_t capacity, int64_t* total);
+
+/* Radius_Search(point, radius, PointVector&) (ikd_Tree.h:238,
+ * ikd_Tree.cpp:406-411), batched: query i uses radius[i * radius_stride]
+ * (radius_stride 0: one radius for all).  CSR output as ikdg_box_search. */
+int ikdg_radius_search(ikdg_tree* t, const float* centers, int64_t nq, int32_t stride, const float* radius,
+                       int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
+                       int64_t* total);
+
+/* size() (ikd_Tree.cpp:78-96): stored points, deleted ones not yet dropped by a
+ * rebuild included.  validnum() (ikd_Tree.cpp:128-145): valid points. */
+int ikdg_size(ikdg_tree* t, int64_t* out);
+int ikdg_validnum(ikdg_tree* t, int64_t* out);
+
+/* tree_range() (ikd_Tree.cpp:98-126): AABB of the valid points (zeros when
+ * the tree is empty). */
+int ikdg_tree_range(ikdg_tree* t, float* box6);
+/* root_alpha() (ikd_Tree.cpp:147-165): balance and deleted share at the root. */
+int ikdg_root_alpha(ikdg_tree* t, float* alpha_bal, float* alpha_del);
+
+/* flatten(Root_Node, Storage, NOT_RECORD) (ikd_Tree.cpp:1325-1352): all valid
+ * points (order unspecified).  IKDG_CAPACITY with *n = required size when
+ * `capacity` is too small.  ids may be NULL. */
+int ikdg_flatten(ikdg_tree* t, float* xyz, int32_t* ids, int64_t capacity, int64_t* n);
+
+/* acquire_removed_points (ikd_Tree.cpp:558-571): drains the points deleted by
+ * box or point deletion that rebuilds have dropped since the last call.
+ * IKDG_CAPACITY with *n = required size (nothing drained) when too small. */
+int ikdg_acquire_removed_points(ikdg_tree* t, float* xyz, int64_t capacity, int64_t* n);
+
+/* Rebuilds the whole tree from its valid points (compaction). */
+int ikdg_rebuild(ikdg_tree* t);
+
+/* Stream control: the tree runs all work on one CUDA stream. */
+int ikdg_get_stream(ikdg_tree* t, void** stream);
+int ikdg_set_stream(ikdg_tree* t, void* stream);
+int ikdg_synchronize(ikdg_tree* t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IKDG_H */

@@ -1,0 +1,204 @@
+"""GPU parity: libikdg (through its C ABI) against the brute-force oracle model.
+
+Every comparison is bit-exact: point ids and float32 squared distances for kNN,
+id sets for box / radius searches, id + coordinate sets of the valid points
+after mutations.  Ties are broken by point id on both sides.
+"""
+import numpy as np
+import pytest
+
+import spec
+
+pytestmark = pytest.mark.gpu
+
+
+def canon_pts(xyz, ids):
+    order = np.argsort(ids, kind="stable")
+    return np.asarray(ids)[order], np.asarray(xyz, np.float32)[order]
+
+
+def assert_same_valid(tree, ref):
+    xyz, ids = tree.flatten(with_ids=True)
+    rxyz, rids = ref.valid_points()
+    a_ids, a_xyz = canon_pts(xyz, ids)
+    b_ids, b_xyz = canon_pts(rxyz, rids)
+    assert np.array_equal(a_ids, b_ids)
+    assert np.array_equal(a_xyz.view(np.uint32), b_xyz.view(np.uint32))
+    assert tree.validnum() == ref.validnum()
+
+
+def assert_knn(tree, ref, q, k, max_dist=np.inf):
+    ids, d2, xyz, cnt = tree.knn(q, k, max_dist)
+    rid, rd2 = ref.knn(q, k, max_dist)
+    assert np.array_equal(ids, rid), f"ids differ for k={k} max_dist={max_dist}"
+    assert np.array_equal(d2.view(np.uint32), rd2.view(np.uint32))
+    assert np.array_equal(cnt, (rid >= 0).sum(1))
+
+
+def assert_ranges(tree, ref, boxes, centres, radii):
+    offs, ids, _ = tree.box_search(boxes)
+    for i, want in enumerate(ref.box_search(boxes)):
+        assert np.array_equal(np.sort(ids[offs[i]:offs[i + 1]]), want)
+    offs, ids, _ = tree.radius_search(centres, radii)
+    for i, want in enumerate(ref.radius_search(centres, radii)):
+        assert np.array_equal(np.sort(ids[offs[i]:offs[i + 1]]), want)
+
+
+def random_boxes(rng, n, lo, hi, smin, smax):
+    c = rng.uniform(lo, hi, (n, 3))
+    s = rng.uniform(smin, smax, (n, 3))
+    return np.concatenate([c - s / 2, c + s / 2], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("n", [1, 17, 1000, 50000])
+def test_knn_uniform(ikdg_mod, n):
+    rng = np.random.default_rng(100 + n)
+    pts = rng.uniform(-20, 20, (n, 3)).astype(np.float32)
+    q = rng.uniform(-22, 22, (1500, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(), spec.SpecTree()
+    tree.Build(pts)
+    ref.Build(pts)
+    for k in (1, 5, 8, 16, 33):
+        assert_knn(tree, ref, q, k)
+    assert_knn(tree, ref, q, 5, 1.0)
+    assert_knn(tree, ref, q, 3, 0.0)
+
+
+def test_knn_ties_broken_by_id(ikdg_mod):
+    # Integer lattice with duplicated points: many exactly equal distances.
+    g = np.stack(np.meshgrid(*[np.arange(-6, 7)] * 3, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    pts = np.concatenate([g, g[::3]])
+    q = np.concatenate([g[::7], g[::11] + 0.5]).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(), spec.SpecTree()
+    tree.Build(pts)
+    ref.Build(pts)
+    for k in (1, 4, 7, 20):
+        assert_knn(tree, ref, q, k)
+
+
+def test_box_and_radius(ikdg_mod):
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(-10, 10, (30000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(), spec.SpecTree()
+    tree.Build(pts)
+    ref.Build(pts)
+    boxes = random_boxes(rng, 200, -12, 12, 0.1, 8)
+    cen = rng.uniform(-12, 12, (200, 3)).astype(np.float32)
+    rad = rng.uniform(0.1, 5, 200).astype(np.float32)
+    assert_ranges(tree, ref, boxes, cen, rad)
+    # boxes snapped onto point coordinates exercise the half-open bounds
+    sel = pts[rng.choice(len(pts), 50)]
+    snapped = np.concatenate([sel, sel + 1.0], 1).astype(np.float32)
+    assert_ranges(tree, ref, snapped, sel, np.float32(0.0))
+
+
+def test_empty_tree(ikdg_mod):
+    tree = ikdg_mod.KDTree()
+    tree.Build(np.zeros((0, 3), np.float32))
+    ids, d2, _, cnt = tree.knn(np.zeros((4, 3), np.float32), 3)
+    assert (ids == -1).all() and np.isinf(d2).all() and (cnt == 0).all()
+    assert tree.size() == 0 and tree.validnum() == 0
+    offs, got, _ = tree.box_search(np.array([[-1, -1, -1, 1, 1, 1]], np.float32))
+    assert offs[-1] == 0
+    assert tree.Delete_Point_Boxes(np.array([[-1, -1, -1, 1, 1, 1]], np.float32)) == 0
+    # Adding to an empty tree works (the reference dereferences a null root).
+    pts = np.random.default_rng(0).uniform(-1, 1, (100, 3)).astype(np.float32)
+    assert tree.Add_Points(pts, False) == 0
+    ref = spec.SpecTree()
+    ref.Build(np.zeros((0, 3), np.float32))
+    ref.Add_Points(pts, False)
+    assert_same_valid(tree, ref)
+    assert_knn(tree, ref, pts[:20], 200)
+
+
+def test_k_exceeds_valid_count(ikdg_mod):
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 2, 0]], np.float32)
+    tree, ref = ikdg_mod.KDTree(), spec.SpecTree()
+    tree.Build(pts)
+    ref.Build(pts)
+    assert_knn(tree, ref, np.array([[0.1, 0.1, 0]], np.float32), 5)
+    assert_knn(tree, ref, np.array([[0.1, 0.1, 0]], np.float32), 5, 1.0)
+
+
+def test_mutation_sequence(ikdg_mod):
+    rng = np.random.default_rng(11)
+    L = 8.0
+    pts = rng.uniform(-L, L, (20000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.3, 0.6, 0.3), spec.SpecTree(0.3)
+    tree.Build(pts)
+    ref.Build(pts)
+    q = rng.uniform(-L, L, (400, 3)).astype(np.float32)
+    for it in range(8):
+        add = rng.uniform(-L, L, (1500, 3)).astype(np.float32)
+        assert tree.Add_Points(add, False) == ref.Add_Points(add, False) == 0
+        cur, _ = ref.valid_points()
+        dels = cur[rng.choice(len(cur), 300, replace=False)]
+        tree.Delete_Points(dels)
+        ref.Delete_Points(dels)
+        boxes = random_boxes(rng, 3, -L, L, 0.5, 4)
+        assert tree.Delete_Point_Boxes(boxes) == ref.Delete_Point_Boxes(boxes)
+        add2 = rng.uniform(-L, L, (800, 3)).astype(np.float32)
+        add2[:100] = cur[rng.choice(len(cur), 100)]
+        assert tree.Add_Points(add2, True) == ref.Add_Points(add2, True)
+        assert_same_valid(tree, ref)
+        assert_knn(tree, ref, q, 5)
+        assert_knn(tree, ref, q, 12, 1.2)
+    assert_ranges(tree, ref, random_boxes(rng, 50, -L, L, 0.5, 6), q[:50], np.float32(1.5))
+
+
+@pytest.mark.parametrize("ds", [0.2, 0.5, 0.37])
+def test_downsample(ikdg_mod, ds):
+    rng = np.random.default_rng(int(ds * 100))
+    base = rng.uniform(-5, 5, (8000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, ds), spec.SpecTree(ds)
+    tree.Build(base)
+    ref.Build(base)
+    for it in range(4):
+        # dense clusters: many new points per voxel, exact duplicates included
+        c = rng.uniform(-5, 5, (40, 3))
+        add = (c[rng.integers(0, 40, 3000)] + rng.normal(0, ds, (3000, 3))).astype(np.float32)
+        add[::17] = add[::17][::-1]
+        add[5::29] = base[rng.choice(len(base), len(add[5::29]))]
+        assert tree.Add_Points(add, True) == ref.Add_Points(add, True)
+        assert_same_valid(tree, ref)
+    assert_knn(tree, ref, rng.uniform(-5, 5, (300, 3)).astype(np.float32), 5)
+
+
+def test_downsample_voxel_boundaries(ikdg_mod):
+    # Coordinates exactly on voxel faces and a 1-ulp neighbourhood of them.
+    ds = 0.2
+    k = np.arange(-20, 20, dtype=np.float32)
+    faces = (k * np.float32(ds)).astype(np.float32)
+    vals = np.concatenate([faces, np.nextafter(faces, np.float32(np.inf)), np.nextafter(faces, -np.float32(np.inf))])
+    rng = np.random.default_rng(5)
+    add = rng.choice(vals, (4000, 3)).astype(np.float32)
+    base = rng.choice(vals, (2000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, ds), spec.SpecTree(ds)
+    tree.Build(base)
+    ref.Build(base)
+    assert tree.Add_Points(add, True) == ref.Add_Points(add, True)
+    assert_same_valid(tree, ref)
+
+
+def test_growth_and_rebalance(ikdg_mod):
+    # All inserts land in one corner: leaf overflow splits, scapegoat rebuilds,
+    # pool growth.
+    rng = np.random.default_rng(9)
+    base = rng.uniform(-50, 50, (5000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, 0.2), spec.SpecTree(0.2)
+    tree.Build(base)
+    ref.Build(base)
+    for it in range(6):
+        add = rng.uniform(40, 50, (20000, 3)).astype(np.float32)
+        tree.Add_Points(add, False)
+        ref.Add_Points(add, False)
+    assert_same_valid(tree, ref)
+    q = rng.uniform(-50, 50, (500, 3)).astype(np.float32)
+    assert_knn(tree, ref, q, 10)
+    box = np.array([[30, 30, 30, 50, 50, 50]], np.float32)
+    assert tree.Delete_Point_Boxes(box) == ref.Delete_Point_Boxes(box)
+    assert_same_valid(tree, ref)
+    assert_knn(tree, ref, q, 10)
+    tree.rebuild()
+    assert tree.size() == tree.validnum()
+    assert_knn(tree, ref, q, 10)
