@@ -122,7 +122,7 @@ __global__ void level_seg_kernel(DevTree t, const float4* __restrict__ pts, cons
     write_child_cnt(t.ncnt, parent, side, cnt, 0);
     int r = atomicAdd(nseg_next, 2);
     if (r + 1 >= max_next) {  // cannot happen with the host's bound; guard anyway
-        atomicOr(&t.st->err, ERR_POOL);
+        atomicOr(&t.st->err, ERR_SEG);
         seginfo[i] = make_int4(-1, 0, 0, 0);
         return;
     }

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -134,6 +135,10 @@ struct Tree {
 
     std::mutex mu;
     std::string err;
+    // IKDG_DEBUG_VALIDATE=1: check the whole tree's structure after every
+    // mutation (slow; for tests and debugging).
+    bool debug_validate = std::getenv("IKDG_DEBUG_VALIDATE") != nullptr;
+    std::string dbg_note;
 
     // ---- lifetime -------------------------------------------------------------
     void init(int dev) {
@@ -229,6 +234,7 @@ struct Tree {
             grow_array(aux.job_off, list_cap, need_list, 0, stream);
             grow_array(aux.job_fill, list_cap, need_list, 0, stream);
             list_cap = need_list;
+            aux.list_cap = need_list;
         }
     }
 
@@ -256,8 +262,24 @@ struct Tree {
     void read_status() {
         CK(cudaMemcpyAsync(st, st_dev, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
-        if (st->err & ERR_POOL) throw Internal{"device pool exhausted"};
-        if (st->err & ERR_LOOP) throw Internal{"device loop cap reached (corrupted tree)"};
+        if (st->err & ERR_ANY_INTERNAL) {
+            int e = st->err;
+            std::string m = "device error:";
+            if (e & ERR_POOL) m += " node pool exhausted;";
+            if (e & ERR_POOL_LEAF) m += " leaf pool exhausted;";
+            if (e & ERR_SEG) m += " builder segment overflow;";
+            if (e & ERR_ROUTE) m += " insertion without root;";
+            if (e & ERR_OVF_JOB) {
+                m += " overflow point outside rebuild jobs [leaf " + std::to_string(st->dbg[1]) + " parent " +
+                     std::to_string(st->dbg[2]) + " fill " + std::to_string(st->dbg[3]) + " job_of_leaf " +
+                     std::to_string(st->dbg[4]) + " dirty " + std::to_string(st->dbg[5]) + " parent_viol " +
+                     std::to_string(st->dbg[6]) + " n_ovf " + std::to_string(st->dbg[7]) + " n_jobs " +
+                     std::to_string(st->n_jobs) + "];";
+            }
+            if (e & ERR_LOOP) m += " loop cap reached;";
+            if (e & ERR_LIST) m += " work list overflow;";
+            throw Internal{m};
+        }
     }
     void zero_fields(size_t off, size_t bytes) {
         CK(cudaMemsetAsync((char*)st_dev + off, 0, bytes, stream));
@@ -266,7 +288,7 @@ struct Tree {
     void reset_counters() {
         zero_fields(offsetof(DevStatus, err), offsetof(DevStatus, root_code) - offsetof(DevStatus, err));
         zero_fields(offsetof(DevStatus, count), 2 * sizeof(long long));
-        zero_fields(offsetof(DevStatus, job_total), sizeof(long long));
+        zero_fields(offsetof(DevStatus, job_total), sizeof(long long) + 8 * sizeof(int));
     }
     void set_status_ll(size_t off, long long v) {
         CK(cudaMemcpyAsync((char*)st_dev + off, &v, sizeof(v), cudaMemcpyHostToDevice, stream));
@@ -331,9 +353,11 @@ struct Tree {
     // After a mutation queued dirty leaves in aux.items: refit, then rebuild
     // the topmost subtrees that violate the criteria (up to three rounds).
     void finish_update(const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
-        int bound = st->leaf_top + st->node_top + 1;
+        int bound = list_cap;
         launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
         launch_clear_dirty(dt, aux, bound, stream);
+        // The dirty list is consumed: the next update starts a fresh one.
+        zero_fields(offsetof(DevStatus, n_items), sizeof(int));
         // Rebuilding a subtree can unbalance its ancestors; each round moves
         // the violations up, so a few rounds settle the tree.
         for (int round = 0; round < 8; ++round) {
@@ -351,11 +375,16 @@ struct Tree {
             if (nj == 0) throw Internal{"violators without a topmost job"};
             run_jobs(nj, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
             zero_fields(offsetof(DevStatus, n_items), sizeof(int));
+            if (debug_validate) {
+                read_status();
+                if (st->n_viol == 0) check_valid("after a rebuild round");
+            }
         }
         zero_fields(offsetof(DevStatus, n_viol), sizeof(int));
         launch_snapshot_root(dt, stream);
         read_status();
         if (st->err & ERR_STACK) throw Internal{"tree deeper than the traversal stack"};
+        if (debug_validate) check_valid("end of update");
         if (st->err & ERR_ID) throw CapacityFail{"point id space exhausted"};
     }
 
@@ -408,6 +437,7 @@ struct Tree {
         if (next_id + n > (long long)MAX_ID + 1) throw CapacityFail{"point id space exhausted"};
         if (downsample && !(ds_size > 0.f && std::isfinite(ds_size))) throw BadArg{"downsample size must be > 0"};
         reset_counters();
+        if (debug_validate) check_valid("start of Add_Points");
         if (!downsample) {
             op.ensure(align_up(sizeof(float) * n * stride) + 2 * align_up(sizeof(float4) * n) +
                           align_up(sizeof(int4) * n),
@@ -449,11 +479,19 @@ struct Tree {
         long long a = 0;
         while (a < n) {
             set_status_ll(offsetof(DevStatus, count), n);
+            if (debug_validate) check_valid("start of a downsampling sub-batch");
             launch_ds_search(dt, n, ds_size, a, d, n_groups, stream);
             read_status();
             long long e = std::min<long long>(std::max<long long>(st->count, a + 1), n);
             zero_fields(offsetof(DevStatus, n_ins), sizeof(int));
             launch_ds_fold(dt, aux, n, a, e, first_id, d, n_groups, stream);
+            if (debug_validate) {
+                read_status();
+                std::string m = "sub-batch [" + std::to_string(a) + "," + std::to_string(e) + ") groups " +
+                                std::to_string(n_groups) + " ins " + std::to_string(st->n_ins) + " items " +
+                                std::to_string(st->n_items);
+                dbg_note = m;
+            }
             if (st->root_code == 0) {
                 read_status();
                 if (st->n_ins > 0) build_root(d.ins, st->n_ins);
@@ -651,6 +689,23 @@ struct Tree {
         launch_select_root_job(dt, aux, stream);
         run_jobs(1, nullptr, nullptr, 0);
         finish_update(nullptr, nullptr, 0);
+    }
+
+    void check_valid(const char* stage) {
+        long long bad = validate();
+        if (bad) {
+            std::string m = std::string("structural validation failed at ") + stage + " (" + dbg_note + "): " +
+                            std::to_string(bad) + " violations; first:";
+            for (int i = 0; i < 7; ++i) m += " " + std::to_string(st->dbg[i]);
+            throw Internal{m};
+        }
+    }
+
+    long long validate() {
+        zero_fields(offsetof(DevStatus, bad), sizeof(long long));
+        launch_validate(dt, (long long*)((char*)st_dev + offsetof(DevStatus, bad)), stream);
+        read_status();
+        return st->bad;
     }
 
     void tree_range(float* box6) {
@@ -906,6 +961,13 @@ int ikdg_acquire_removed_points(ikdg_tree* h, float* xyz, int64_t capacity, int6
 
 int ikdg_rebuild(ikdg_tree* h) {
     return guarded(h, [&](ikdg::Tree& t) { t.rebuild_all(); });
+}
+
+int ikdg_debug_validate(ikdg_tree* h, int64_t* violations) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long v = t.validate();
+        if (violations) *violations = v;
+    });
 }
 
 int ikdg_get_stream(ikdg_tree* h, void** stream) {

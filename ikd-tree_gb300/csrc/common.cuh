@@ -39,6 +39,12 @@ constexpr int ERR_OUTPUT = 4;      // an output capacity was exceeded
 constexpr int ERR_ID = 8;          // point id space exhausted
 constexpr int ERR_INPUT = 16;      // non-finite input coordinate
 constexpr int ERR_LOOP = 32;       // a bounded device loop hit its cap
+constexpr int ERR_POOL_LEAF = 64;  // leaf pool exhausted
+constexpr int ERR_SEG = 128;       // builder segment list overflow
+constexpr int ERR_ROUTE = 256;     // insertion into a tree without root
+constexpr int ERR_OVF_JOB = 512;   // overflow point outside every rebuild job
+constexpr int ERR_LIST = 1024;     // a work list would exceed its capacity
+constexpr int ERR_ANY_INTERNAL = ERR_POOL | ERR_LOOP | ERR_POOL_LEAF | ERR_SEG | ERR_ROUTE | ERR_OVF_JOB | ERR_LIST;
 
 // Caps on every device loop that follows tree links: a walk to the root takes
 // at most MAX_WALK steps, a traversal at most MAX_VISITS node / leaf visits.
@@ -75,6 +81,8 @@ struct DevStatus {
     long long count2;
     long long removed_n;  // deleted points dropped by rebuilds, not yet drained
     long long job_total;  // points gathered for rebuild jobs
+    int dbg[8];           // details of the first internal error (diagnostics)
+    long long bad;        // structural violations found by the validator
 };
 
 struct DevTree {
@@ -258,7 +266,7 @@ __device__ __forceinline__ int alloc_leaf(const DevTree& t) {
     if (k < t.st->free_leaf_n) return t.free_leaf[t.st->free_leaf_n - 1 - k];
     int n = atomicAdd(&t.st->leaf_top, 1);
     if (n >= t.leaf_cap) {
-        atomicOr(&t.st->err, ERR_POOL);
+        atomicOr(&t.st->err, ERR_POOL_LEAF);
         return -1;
     }
     return n;

@@ -27,11 +27,17 @@ inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) /
 
 __device__ __forceinline__ float coord4(const float4& p, int a) { return a == 0 ? p.x : (a == 1 ? p.y : p.z); }
 
+// Appends `v` to a work list, or flags ERR_LIST when the list is full.
+__device__ __forceinline__ void list_push(DevStatus* st, int* counter, int* list, int cap, int v) {
+    int i = atomicAdd(counter, 1);
+    if (i < cap)
+        list[i] = v;
+    else
+        atomicOr(&st->err, ERR_LIST);
+}
+
 __device__ __forceinline__ void mark_dirty(const UpdateAux& a, DevStatus* st, int L) {
-    if (atomicExch(&a.dirty_flag[L], 1) == 0) {
-        int i = atomicAdd(&st->n_items, 1);
-        a.items[i] = leaf_code(L);
-    }
+    if (atomicExch(&a.dirty_flag[L], 1) == 0) list_push(st, &st->n_items, a.items, a.list_cap, leaf_code(L));
 }
 
 // ---- insertion -----------------------------------------------------------------
@@ -44,7 +50,7 @@ __global__ void route_append_kernel(DevTree t, UpdateAux a, const float4* __rest
     float4 p = pts[i];
     int code = __float_as_int(t.node[3].x);  // sentinel's left child = root
     if (code == 0) {
-        atomicOr(&t.st->err, ERR_POOL);
+        atomicOr(&t.st->err, ERR_ROUTE);
         return;
     }
     int steps = 0;
@@ -73,7 +79,7 @@ __global__ void route_append_kernel(DevTree t, UpdateAux a, const float4* __rest
 
 __global__ void refit_mark_kernel(DevTree t, UpdateAux a, const int* __restrict__ items, const int* n_items) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_items) return;
+    if (i >= *n_items || i >= a.list_cap) return;
     int code = items[i];
     int X;
     if (code < 0) {
@@ -106,7 +112,7 @@ __device__ __forceinline__ int log2_ceil(int x) {
 __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restrict__ items, const int* n_items,
                                      Criteria c, int fill) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_items) return;
+    if (i >= *n_items || i >= a.list_cap) return;
     int code = items[i];
     int X;
     if (code < 0) {
@@ -128,10 +134,8 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         X = lp >> 1;
         write_child_box(t.node, X, lp & 1, b);
         write_child_cnt(t.ncnt, X, lp & 1, n, del);
-        if (n > LEAF_CAP) {  // an overflowing bucket must be split
-            int v = atomicAdd(&t.st->n_viol, 1);
-            a.viol[v] = code;
-        }
+        if (n > LEAF_CAP)  // an overflowing bucket must be split
+            list_push(t.st, &t.st->n_viol, a.viol, a.list_cap, code);
     } else {
         X = code;
     }
@@ -165,8 +169,7 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         if (h > 2 * ideal + 8) viol = true;
         if (viol) {
             a.viol_flag[X] = 1;
-            int v = atomicAdd(&t.st->n_viol, 1);
-            a.viol[v] = X;
+            list_push(t.st, &t.st->n_viol, a.viol, a.list_cap, X);
         }
         int lp = t.nparent[X];
         int P = lp >> 1;
@@ -178,7 +181,7 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
 
 __global__ void clear_dirty_kernel(UpdateAux a, const int* n_items) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_items) return;
+    if (i >= *n_items || i >= a.list_cap) return;
     int code = a.items[i];
     if (code < 0) a.dirty_flag[code_leaf(code)] = 0;
 }
@@ -187,7 +190,7 @@ __global__ void clear_dirty_kernel(UpdateAux a, const int* n_items) {
 
 __global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_viol) return;
+    if (i >= *n_viol || i >= a.list_cap) return;
     int code = a.viol[i];
     int link = code < 0 ? t.lparent[code_leaf(code)] : t.nparent[code];
     if (link < 0) return;
@@ -201,6 +204,10 @@ __global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
         X = t.nparent[X] >> 1;
     }
     int j = atomicAdd(&t.st->n_jobs, 1);
+    if (j >= a.list_cap) {
+        atomicOr(&t.st->err, ERR_LIST);
+        return;
+    }
     a.jobs[j] = code;
     a.job_link[j] = link;
     if (code < 0)
@@ -211,7 +218,7 @@ __global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
 
 __global__ void clear_viol_kernel(UpdateAux a, const int* n_viol) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_viol) return;
+    if (i >= *n_viol || i >= a.list_cap) return;
     int code = a.viol[i];
     if (code > 0) a.viol_flag[code] = 0;
 }
@@ -265,9 +272,22 @@ __global__ void job_count_node_kernel(DevTree t, UpdateAux a, int node_top) {
 __global__ void job_count_ovf_kernel(DevTree t, UpdateAux a, const int4* __restrict__ ovf_leaf, const int* n_ovf) {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= *n_ovf) return;
-    int j = a.leaf_job[ovf_leaf[o].x];
+    int L = ovf_leaf[o].x;
+    int j = a.leaf_job[L];
     if (j < 0) {
-        atomicOr(&t.st->err, ERR_POOL);
+        if (atomicOr(&t.st->err, ERR_OVF_JOB) == 0 || true) {
+            int* d = t.st->dbg;
+            if (atomicCAS(&d[0], 0, 1) == 0) {
+                d[1] = L;
+                d[2] = t.lparent[L];
+                d[3] = t.leaf_n[L];
+                d[4] = a.job_of_leaf[L];
+                d[5] = a.dirty_flag[L];
+                int lp = t.lparent[L];
+                d[6] = lp >= 0 ? a.viol_flag[lp >> 1] : -7;
+                d[7] = *n_ovf;
+            }
+        }
         return;
     }
     atomicAdd(&a.job_count[j], 1);
@@ -347,10 +367,7 @@ __global__ void job_finish_kernel(DevTree t, UpdateAux a, const int* n_jobs) {
     a.job_count[j] = 0;
     a.job_fill[j] = 0;
     int P = a.job_link[j] >> 1;
-    if (P > 0) {
-        int i = atomicAdd(&t.st->n_items, 1);
-        a.items[i] = P;
-    }
+    if (P > 0) list_push(t.st, &t.st->n_items, a.items, a.list_cap, P);
 }
 
 // ---- box / point deletion, box re-insertion ----------------------------------------
@@ -554,6 +571,126 @@ __global__ void select_root_job_kernel(DevTree t, UpdateAux a) {
     else
         a.job_of_node[code] = 0;
     t.st->n_jobs = 1;
+}
+
+// ---- structural validation (diagnostics) ---------------------------------------------
+
+__device__ __forceinline__ bool same_box(const Box3& a, const Box3& b) {
+    for (int k = 0; k < 3; ++k)
+        if (__float_as_uint(a.lo[k]) != __float_as_uint(b.lo[k]) || __float_as_uint(a.hi[k]) != __float_as_uint(b.hi[k]))
+            return false;
+    return true;
+}
+
+// For every live node: both children exist and point back; the child box and
+// counts stored in the node equal what the child itself holds.
+__device__ __forceinline__ void note_bad(DevStatus* st, int kind, int X, int side, int a0, int a1, int a2, int a3) {
+    if (atomicCAS(&st->dbg[0], 0, kind) == 0) {
+        st->dbg[1] = X;
+        st->dbg[2] = side;
+        st->dbg[3] = a0;
+        st->dbg[4] = a1;
+        st->dbg[5] = a2;
+        st->dbg[6] = a3;
+    }
+}
+
+// For every live node: both children exist and point back; the child box and
+// counts stored in the node equal what the child itself holds.
+__global__ void validate_nodes_kernel(DevTree t, unsigned long long* bad) {
+    int X = blockIdx.x * blockDim.x + threadIdx.x;
+    if (X >= t.st->node_top) return;
+    if (X > 0 && t.nparent[X] < 0) return;
+    NodeRec r = load_node_cg(t.node, X);
+    int4 cc = __ldcg(t.ncnt + X);
+    unsigned long long nbad = 0;
+    for (int side = 0; side < 2; ++side) {
+        int c = side == 0 ? r.left() : r.right();
+        int slots = side == 0 ? cc.x : cc.z, del = side == 0 ? cc.y : cc.w;
+        Box3 stored = r.box(side);
+        if (X == 0 && side == 1) {
+            if (c != 0) {
+                ++nbad;
+                note_bad(t.st, 101, X, side, c, 0, 0, 0);
+            }
+            continue;
+        }
+        if (c == 0) {
+            if (X != 0) {  // only an empty tree has no root
+                ++nbad;
+                note_bad(t.st, 102, X, side, 0, 0, 0, 0);
+            }
+            continue;
+        }
+        Box3 b = empty_box();
+        int s2 = 0, d2 = 0;
+        if (c > 0) {
+            if (c >= t.st->node_top || t.nparent[c] != X * 2 + side) {
+                ++nbad;
+                note_bad(t.st, 103, X, side, c, c < t.st->node_top ? t.nparent[c] : -9, 0, 0);
+                continue;
+            }
+            NodeRec rc = load_node_cg(t.node, c);
+            int4 c4 = __ldcg(t.ncnt + c);
+            Box3 bl = rc.box(0), br = rc.box(1);
+            if (!box_empty(bl)) box_union(b, bl);
+            if (!box_empty(br)) box_union(b, br);
+            s2 = c4.x + c4.z;
+            d2 = c4.y + c4.w;
+        } else {
+            int L = code_leaf(c);
+            if (L >= t.st->leaf_top || t.lparent[L] != X * 2 + side) {
+                ++nbad;
+                note_bad(t.st, 104, X, side, c, L < t.st->leaf_top ? t.lparent[L] : -9, 0, 0);
+                continue;
+            }
+            int n = t.leaf_n[L];
+            if (n > LEAF_CAP || n < 0) {
+                ++nbad;
+                note_bad(t.st, 105, X, side, c, n, 0, 0);
+                continue;
+            }
+            s2 = n;
+            for (int j = 0; j < n; ++j) {
+                float4 p = __ldcg(t.pts + (long long)L * LEAF_CAP + j);
+                if (__float_as_uint(p.w) & F_DEL)
+                    ++d2;
+                else
+                    box_grow(b, p.x, p.y, p.z);
+            }
+        }
+        if (s2 != slots || d2 != del) {
+            ++nbad;
+            note_bad(t.st, 106, X, side, slots, s2, del, d2);
+        } else if (!same_box(b, stored)) {
+            ++nbad;
+            int k = 0;
+            while (k < 3 && __float_as_uint(b.lo[k]) == __float_as_uint(stored.lo[k]) &&
+                   __float_as_uint(b.hi[k]) == __float_as_uint(stored.hi[k]))
+                ++k;
+            note_bad(t.st, 107, X, side, c, k, __float_as_int(k < 3 ? b.lo[k] : 0.f),
+                     __float_as_int(k < 3 ? stored.lo[k] : 0.f));
+        }
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+// Every live leaf is the child its parent record names.
+__global__ void validate_leaves_kernel(DevTree t, unsigned long long* bad) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= t.st->leaf_top) return;
+    int lp = t.lparent[L];
+    if (lp < 0) return;
+    int P = lp >> 1;
+    bool ok = P < t.st->node_top && (P == 0 || t.nparent[P] >= 0);
+    if (ok) {
+        const int* codes = reinterpret_cast<const int*>(t.node + 4 * P + 3);
+        ok = codes[lp & 1] == leaf_code(L);
+    }
+    if (!ok) {
+        atomicAdd(bad, 1ull);
+        note_bad(t.st, 108, P, lp & 1, L, lp, 0, 0);
+    }
 }
 
 __global__ void snapshot_root_kernel(DevTree t) {
@@ -961,6 +1098,13 @@ void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts
 }
 
 void launch_snapshot_root(const DevTree& t, cudaStream_t s) { snapshot_root_kernel<<<1, 1, 0, s>>>(t); }
+
+void launch_validate(const DevTree& t, long long* bad, cudaStream_t s) {
+    if (t.node_cap > 0)
+        validate_nodes_kernel<<<blocks_for(t.node_cap, 256), 256, 0, s>>>(t, (unsigned long long*)bad);
+    if (t.leaf_cap > 0)
+        validate_leaves_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, (unsigned long long*)bad);
+}
 
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s) {
     if (t.leaf_cap <= 0) return;

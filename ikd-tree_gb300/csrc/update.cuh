@@ -22,6 +22,7 @@ struct UpdateAux {
     int* job_count;     // [leaf_cap + node_cap + 1]
     int* job_off;       // [leaf_cap + node_cap + 1]
     int* job_fill;      // [leaf_cap + node_cap]
+    int list_cap;       // entries of items / viol / jobs / job_link
 };
 
 struct Criteria {
@@ -66,6 +67,8 @@ void launch_pack_points(const DevTree& t, const float* in, int stride, long long
 void launch_check_finite(const DevTree& t, const float* in, long long count, cudaStream_t s);
 // Copies every valid point ({x, y, z, id}) to out; *counter += count.
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s);
+// Structural check of the whole tree; *bad += number of violations.
+void launch_validate(const DevTree& t, long long* bad, cudaStream_t s);
 // Makes the whole tree the single rebuild job (st->n_jobs = 1).
 void launch_select_root_job(const DevTree& t, const UpdateAux& a, cudaStream_t s);
 

@@ -52,6 +52,7 @@ SIGNATURES = {
     "ikdg_flatten": (C.c_int, [_vp, _fp, _ip, C.c_int64, _lp]),
     "ikdg_acquire_removed_points": (C.c_int, [_vp, _fp, C.c_int64, _lp]),
     "ikdg_rebuild": (C.c_int, [_vp]),
+    "ikdg_debug_validate": (C.c_int, [_vp, _lp]),
     "ikdg_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "ikdg_set_stream": (C.c_int, [_vp, _vp]),
     "ikdg_synchronize": (C.c_int, [_vp]),
@@ -280,6 +281,12 @@ class KDTree:
         xyz = np.empty((k, 3), np.float32)
         self._check(self.lib.ikdg_acquire_removed_points(self.h, _p(xyz), k, C.byref(n)), "acquire_removed_points")
         return xyz
+
+    def validate(self) -> int:
+        """Structural violations of the device tree (0 = sound)."""
+        n = C.c_int64(0)
+        self._check(self.lib.ikdg_debug_validate(self.h, C.byref(n)), "debug_validate")
+        return n.value
 
     # -- streams ---------------------------------------------------------------
     def stream(self) -> int:

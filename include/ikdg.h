@@ -138,6 +138,11 @@ int ikdg_acquire_removed_points(ikdg_tree* t, float* xyz, int64_t capacity, int6
 /* Rebuilds the whole tree from its valid points (compaction). */
 int ikdg_rebuild(ikdg_tree* t);
 
+/* Diagnostics (no counterpart in the reference): checks the device tree's
+ * structure - parent / child links, per-child counts and AABBs, leaf fill - and
+ * reports the number of violations (0 for a sound tree). */
+int ikdg_debug_validate(ikdg_tree* t, int64_t* violations);
+
 /* Stream control: the tree runs all work on one CUDA stream. */
 int ikdg_get_stream(ikdg_tree* t, void** stream);
 int ikdg_set_stream(ikdg_tree* t, void* stream);

@@ -153,3 +153,7 @@ class SpecTree:
 
     def validnum(self) -> int:
         return int(self.valid.sum())
+
+    def size(self) -> int:
+        """Stored points; the model never drops deleted ones (tree-shape dependent)."""
+        return int(len(self.pts))

@@ -3,6 +3,10 @@ import sys
 
 import pytest
 
+# Every tree created by the tests checks its whole device structure (links,
+# per-child counts and AABBs) after each mutation.
+os.environ.setdefault("IKDG_DEBUG_VALIDATE", "1")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 for sub in ("ikd-tree_gb300", "oracle"):
     p = os.path.join(ROOT, sub)
