@@ -250,16 +250,28 @@ def run_ours(args):
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = statistics.mean(step_ms)
 
-    # ---- e2e: host buffers through ikdg_knn (H2D + kernel + D2H inside)
+    # ---- e2e: pinned host buffers through the C ABI (ikdg_knn): the queries
+    # come from host memory and ids, squared distances, points and counts go
+    # back to host memory inside the timed call.
+    qpin = [torch.from_numpy(q).pin_memory() for q in qhost]
+    h_ids = torch.empty((N_Q, K), dtype=torch.int32).pin_memory()
+    h_d2 = torch.empty((N_Q, K), dtype=torch.float32).pin_memory()
+    h_xyz = torch.empty((N_Q, K, 3), dtype=torch.float32).pin_memory()
+    h_cnt = torch.empty((N_Q,), dtype=torch.int32).pin_memory()
+
+    def host_step(s):
+        tree.knn_into(qpin[s].data_ptr(), N_Q, K, math.inf, h_ids.data_ptr(), h_d2.data_ptr(), h_xyz.data_ptr(),
+                      h_cnt.data_ptr())
+
     for s in range(W):
-        tree.knn(qhost[s], K, math.inf)
+        host_step(s)
     e2e_ms = []
     for s in range(Kst):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        tree.knn(qhost[W + s], K, math.inf)
+        host_step(W + s)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_step = statistics.mean(e2e_ms)
 
@@ -288,7 +300,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K, "max_dist": "inf",
                    "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "queries/s", "ms_per_step": e2e_step,
-                "h2d_bytes_per_step": N_Q * 12, "d2h_bytes_per_step": N_Q * K * (4 + 4 + 12 + 0) + N_Q * 4},
+                "h2d_bytes_per_step": N_Q * 12, "d2h_bytes_per_step": N_Q * K * (4 + 4 + 12) + N_Q * 4,
+                "host_buffers": "pinned"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": knn_traffic(), "peak_source": peak_kind,
                      "bytes_per_query": bytes_per_query(N_MAP, K)},

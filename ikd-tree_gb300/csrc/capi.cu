@@ -122,6 +122,13 @@ struct Tree {
     float del_param = 0.5f, bal_param = 0.6f, ds_size = 0.2f;
     int fill = 16;
     int min_size = 2 * LEAF_CAP;
+    int knn_lanes = 1;     // threads per kNN query (1, 2 or 4)
+    int knn_bin_bits = 0;  // tree levels used to order kNN queries (0 = off)
+    // On Grace-Blackwell the GPU reads and writes pageable host memory through
+    // NVLink-C2C with the CPU's page tables (cudaDevAttrPageableMemoryAccess).
+    // Host-pointer searches then run their kernels directly on the caller's
+    // buffers instead of staging copies.  IKDG_HOST_STAGING=1 forces copies.
+    int host_mode = 0;  // 0: staging copies, 1: direct reads + staged results, 2: all direct
 
     DevTree dt{};
     UpdateAux aux{};
@@ -151,6 +158,14 @@ struct Tree {
         std::memset(st, 0, sizeof(DevStatus));
         CK(cudaMemsetAsync(st_dev, 0, sizeof(DevStatus), stream));
         dt.st = st_dev;
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+            cudaGetLastError();
+            pageable = 0;
+        }
+        host_mode = pageable != 0 ? 1 : 0;
+        if (const char* m = std::getenv("IKDG_HOST_MODE")) host_mode = pageable != 0 ? std::atoi(m) : 0;
+        if (std::getenv("IKDG_HOST_STAGING") != nullptr) host_mode = 0;
         ensure_pools(64, 64);
         reset_tree();
         CK(cudaStreamSynchronize(stream));
@@ -325,6 +340,17 @@ struct Tree {
     // gather their valid points (plus overflow points), rebuild, relink and
     // refit their ancestors.
     void run_jobs(int nj, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+        if (debug_validate) {
+            std::vector<int> jobs(nj), links(nj);
+            CK(cudaMemcpyAsync(jobs.data(), aux.jobs, sizeof(int) * nj, cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(links.data(), aux.job_link, sizeof(int) * nj, cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            std::vector<int> sl(links);
+            std::sort(sl.begin(), sl.end());
+            for (int i = 1; i < nj; ++i)
+                if (sl[i] == sl[i - 1])
+                    throw Internal{"two rebuild jobs share the link " + std::to_string(sl[i]) + " (" + dbg_note + ")"};
+        }
         small.ensure(scan_temp_bytes(nj + 1) + 1024, stream);
         launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, nj, small.p, stream);
         read_status();
@@ -352,10 +378,12 @@ struct Tree {
 
     // After a mutation queued dirty leaves in aux.items: refit, then rebuild
     // the topmost subtrees that violate the criteria (up to three rounds).
-    void finish_update(const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+    void finish_update(const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound, bool refit_first = true) {
         int bound = list_cap;
-        launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
-        launch_clear_dirty(dt, aux, bound, stream);
+        if (refit_first) {
+            launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
+            launch_clear_dirty(dt, aux, bound, stream);
+        }
         // The dirty list is consumed: the next update starts a fresh one.
         zero_fields(offsetof(DevStatus, n_items), sizeof(int));
         // Rebuilding a subtree can unbalance its ancestors; each round moves
@@ -552,18 +580,22 @@ struct Tree {
         float lim = max_sq_threshold(max_dist);
         size_t nk = (size_t)nq * k;
         if (device_ptrs) {
-            int* slots = nullptr;
-            if (k > KNN_REG_MAX) {
-                small.ensure(align_up(sizeof(int) * nk), stream);
-                slots = (int*)small.p;
-            }
-            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, slots, stream);
+            small.ensure(knn_temp_bytes(nq, k) + 256, stream);
+            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, small.p, knn_lanes, knn_bin_bits, stream);
             CK(cudaGetLastError());
             return;
         }
         reset_counters();
+        if (host_mode == 2) {
+            // Kernels read the queries and write the results in host memory.
+            small.ensure(knn_temp_bytes(nq, k) + 256, stream);
+            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, small.p, knn_lanes, knn_bin_bits, stream);
+            read_status();
+            if (st->err & ERR_STACK) throw Internal{"knn: traversal stack overflow"};
+            return;
+        }
         op.ensure(align_up(sizeof(float) * nq * stride) + align_up(sizeof(int) * nk) + align_up(sizeof(float) * nk) +
-                      align_up(sizeof(float) * nk * 3) + align_up(sizeof(int) * nq) + align_up(sizeof(int) * nk),
+                      align_up(sizeof(float) * nk * 3) + align_up(sizeof(int) * nq) + align_up(knn_temp_bytes(nq, k)),
                   stream);
         Carver c(op.p);
         float* dq = c.take<float>((size_t)nq * stride);
@@ -571,9 +603,15 @@ struct Tree {
         float* dd2 = c.take<float>(nk);
         float* dxyz = xyz ? c.take<float>(nk * 3) : nullptr;
         int* dcnt = cnt ? c.take<int>(nq) : nullptr;
-        int* slots = k > KNN_REG_MAX ? c.take<int>(nk) : nullptr;
-        CK(cudaMemcpyAsync(dq, q, sizeof(float) * nq * stride, cudaMemcpyHostToDevice, stream));
-        launch_knn(dt, dq, stride, nq, k, lim, dids, dd2, dxyz, dcnt, slots, stream);
+        char* temp = c.take<char>(knn_temp_bytes(nq, k));
+        // Mode 1: the kernel reads the (small, in-order) queries straight from
+        // host memory; the results come back by DMA.
+        const float* qsrc = q;
+        if (host_mode == 0) {
+            CK(cudaMemcpyAsync(dq, q, sizeof(float) * nq * stride, cudaMemcpyHostToDevice, stream));
+            qsrc = dq;
+        }
+        launch_knn(dt, qsrc, stride, nq, k, lim, dids, dd2, dxyz, dcnt, temp, knn_lanes, knn_bin_bits, stream);
         CK(cudaMemcpyAsync(ids, dids, sizeof(int) * nk, cudaMemcpyDeviceToHost, stream));
         CK(cudaMemcpyAsync(d2, dd2, sizeof(float) * nk, cudaMemcpyDeviceToHost, stream));
         if (xyz) CK(cudaMemcpyAsync(xyz, dxyz, sizeof(float) * nk * 3, cudaMemcpyDeviceToHost, stream));
@@ -688,7 +726,8 @@ struct Tree {
         reset_counters();
         launch_select_root_job(dt, aux, stream);
         run_jobs(1, nullptr, nullptr, 0);
-        finish_update(nullptr, nullptr, 0);
+        // run_jobs already refit the root's parent (the sentinel: nothing to do)
+        finish_update(nullptr, nullptr, 0, /*refit_first=*/false);
     }
 
     void check_valid(const char* stage) {
@@ -839,6 +878,20 @@ int ikdg_set_leaf_fill(ikdg_tree* h, int fill) {
     return guarded(h, [&](ikdg::Tree& t) {
         if (fill < 4 || fill > ikdg::LEAF_CAP) throw ikdg::BadArg{"leaf fill must be in [4, 32]"};
         t.fill = fill;
+    });
+}
+
+int ikdg_set_knn_lanes(ikdg_tree* h, int lanes) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (lanes != 1 && lanes != 2 && lanes != 4) throw ikdg::BadArg{"kNN lanes must be 1, 2 or 4"};
+        t.knn_lanes = lanes;
+    });
+}
+
+int ikdg_set_knn_bin_bits(ikdg_tree* h, int bits) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (bits < 0 || bits > ikdg::QBIN_BITS) throw ikdg::BadArg{"kNN bin bits must be in [0, 16]"};
+        t.knn_bin_bits = bits;
     });
 }
 

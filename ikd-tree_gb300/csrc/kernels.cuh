@@ -46,10 +46,20 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
                     int njobs, long long max_job, int fill, const BuildScratch& bs, cudaStream_t s);
 
 // ---- query.cu ---------------------------------------------------------------
-// k > 64 needs `slots`: k ints of device scratch per query (else nullptr).
+// Batched kNN.  `temp` must hold knn_temp_bytes(nq, k) bytes of device
+// scratch: the query binning (QBIN_BINS counters, a key and a permutation
+// entry per query, for batches of at least QBIN_MIN_QUERIES) and, for
+// k > KNN_REG_MAX, k slot indices per query.
 constexpr int KNN_REG_MAX = 64;
+constexpr int QBIN_BITS = 16;
+constexpr int QBIN_BINS = 1 << QBIN_BITS;
+constexpr long long QBIN_MIN_QUERIES = 2048;
+size_t knn_temp_bytes(long long nq, int k);
+// `lanes` (1, 2 or 4) threads cooperate on each query; `bin_bits` (0 = off,
+// at most QBIN_BITS) levels of the tree order the queries before the search.
 void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq,
-                int* out_id, float* out_d2, float* out_xyz, int* out_cnt, int* slots, cudaStream_t s);
+                int* out_id, float* out_d2, float* out_xyz, int* out_cnt, void* temp, int lanes, int bin_bits,
+                cudaStream_t s);
 // Box (mode 0) and radius (mode 1) search.  Pass 1 (ids == nullptr) writes
 // per-query hit counts into `counts`; pass 2 writes ids / xyz starting at
 // offsets[i].  Boxes are {min xyz, max xyz}; radius queries are {x, y, z} with

@@ -29,14 +29,32 @@ __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
 // KMAX == 0: any k; the sorted candidates live in the query's output rows
 // (global memory), with the slot index parked in out_cnt-independent scratch
 // `slots` (k ints per query).
-template <int KMAX>
+// Traversal of one query by a group of G consecutive lanes: nearer child
+// first, the farther one pushed with its box distance; a subtree is skipped
+// when that distance exceeds min(max_dist^2, current k-th distance).  The loop
+// is "while-while": a node phase steps every group through nodes until it holds
+// a leaf (or is finished), then the warp scans leaves together, so the leaf
+// scans run with most lanes active.  The G lanes of a group keep identical
+// copies of the traversal state; in a leaf, lane s takes slots s, s+G, ...
+// and the G candidates of each round are broadcast and offered to every copy
+// in lane order, which keeps the copies identical.
+template <int KMAX, int G>
 __global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
                                                   long long nq, int k, float max_sq, int* __restrict__ out_id,
                                                   float* __restrict__ out_d2, float* __restrict__ out_xyz,
-                                                  int* __restrict__ out_cnt, int* __restrict__ slots) {
-    long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= nq) return;
-    const float qx = q[qi * q_stride + 0], qy = q[qi * q_stride + 1], qz = q[qi * q_stride + 2];
+                                                  int* __restrict__ out_cnt, int* __restrict__ slots,
+                                                  const int* __restrict__ perm) {
+    const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tid = gtid / G;
+    const int sub = threadIdx.x & (G - 1);
+    const int lane = threadIdx.x & 31;
+    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+    const bool valid = tid < nq;
+    long long qi = valid ? tid : 0;
+    if (valid && perm != nullptr) qi = __ldg(perm + tid);
+    const float qx = valid ? q[qi * q_stride + 0] : 0.f;
+    const float qy = valid ? q[qi * q_stride + 1] : 0.f;
+    const float qz = valid ? q[qi * q_stride + 2] : 0.f;
 
     constexpr int KR = KMAX > 0 ? KMAX : 1;
     float bd[KR];
@@ -57,16 +75,83 @@ __global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __rest
     int st_code[MAX_STACK];
     float st_d[MAX_STACK];
     int sp = 0;
-    int cur = 0;  // start at the sentinel record (node 0)
-    const float4* __restrict__ P = t.pts;
+    int cur = 0;  // node code (>= 0; 0 = the sentinel record) or leaf code (< 0)
+    bool done = !valid;
     int visits = 0;
+    const float4* __restrict__ P = t.pts;
+
+    // Next stacked subtree that can still hold a result, or done.
+    auto pop = [&]() {
+        const float lim = fminf(max_sq, worst);
+        while (sp > 0) {
+            --sp;
+            if (st_d[sp] <= lim) {
+                cur = st_code[sp];
+                return;
+            }
+        }
+        done = true;
+    };
+
+    // Offers a candidate to this lane's copy of the k best.
+    auto offer = [&](float d, int id, int sl) {
+        if (!(d <= max_sq && cand_less(d, id, worst, worst_id))) return;
+        if (KMAX == 0) {
+            // Large k: the sorted list lives in the output rows; only the
+            // group's first lane owns them.
+            if (sub == 0) {
+                int pos = gcnt < k ? gcnt : k - 1;
+                while (pos > 0 && cand_less(d, id, gd[pos - 1], gi[pos - 1])) {
+                    gd[pos] = gd[pos - 1];
+                    gi[pos] = gi[pos - 1];
+                    gs[pos] = gs[pos - 1];
+                    --pos;
+                }
+                gd[pos] = d;
+                gi[pos] = id;
+                gs[pos] = sl;
+            }
+            if (gcnt < k) ++gcnt;
+            if (gcnt == k) {
+                __syncwarp(gmask);
+                worst = __shfl_sync(gmask, sub == 0 ? gd[k - 1] : 0.f, lane & ~(G - 1));
+                worst_id = __shfl_sync(gmask, sub == 0 ? gi[k - 1] : 0, lane & ~(G - 1));
+            }
+            return;
+        }
+        float cd = d;
+        int cid = id, cs = sl;
+#pragma unroll
+        for (int m = 0; m < KR; ++m) {
+            const bool sw = cand_less(cd, cid, bd[m], bi[m]);
+            const float td = bd[m];
+            const int ti = bi[m], ts = bsl[m];
+            bd[m] = sw ? cd : td;
+            bi[m] = sw ? cid : ti;
+            bsl[m] = sw ? cs : ts;
+            cd = sw ? td : cd;
+            cid = sw ? ti : cid;
+            cs = sw ? ts : cs;
+        }
+#pragma unroll
+        for (int m = 0; m < KR; ++m)
+            if (m == k - 1) {
+                worst = bd[m];
+                worst_id = bi[m];
+            }
+    };
 
     while (true) {
-        if (++visits > MAX_VISITS) {
-            atomicOr(&t.st->err, ERR_LOOP);
-            break;
-        }
-        if (cur >= 0) {
+        // Node phase.
+        while (true) {
+            const bool nodework = !done && cur >= 0;
+            if (!__any_sync(0xffffffffu, nodework)) break;
+            if (!nodework) continue;
+            if (++visits > MAX_VISITS) {
+                atomicOr(&t.st->err, ERR_LOOP);
+                done = true;
+                continue;
+            }
             NodeRec r = load_node(t.node, cur);
             const int cl = r.left(), cr = r.right();
             const float lim = fminf(max_sq, worst);
@@ -90,81 +175,50 @@ __global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __rest
                     atomicOr(&t.st->err, ERR_STACK);
                 }
                 cur = left_first ? cl : cr;
-                continue;
-            }
-            if (vl) {
+            } else if (vl) {
                 cur = cl;
-                continue;
-            }
-            if (vr) {
+            } else if (vr) {
                 cur = cr;
-                continue;
+            } else {
+                pop();
             }
-        } else {
-            const int L = code_leaf(cur);
-            const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
-            const float4* lp = P + (long long)L * LEAF_CAP;
-            for (int j = 0; j < n; ++j) {
+        }
+        // Leaf phase.
+        const bool leafwork = !done && cur < 0;
+        if (!__any_sync(0xffffffffu, leafwork)) break;
+        if (!leafwork) continue;
+        const int L = code_leaf(cur);
+        const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
+        const float4* lp = P + (long long)L * LEAF_CAP;
+        for (int j0 = 0; j0 < n; j0 += G) {
+            const int j = j0 + sub;
+            float d = FINF;
+            int id = 0x7fffffff, sl = -1;
+            if (j < n) {
                 const float4 p = __ldg(lp + j);
                 const uint32_t w = __float_as_uint(p.w);
-                if (w & F_DEL) continue;
-                const float d = sq_dist(qx, qy, qz, p.x, p.y, p.z);
-                const int id = (int)(w & ID_MASK);
-                if (d <= max_sq && cand_less(d, id, worst, worst_id)) {
-                    if (KMAX == 0) {
-                        int pos = gcnt < k ? gcnt : k - 1;
-                        while (pos > 0 && cand_less(d, id, gd[pos - 1], gi[pos - 1])) {
-                            gd[pos] = gd[pos - 1];
-                            gi[pos] = gi[pos - 1];
-                            gs[pos] = gs[pos - 1];
-                            --pos;
-                        }
-                        gd[pos] = d;
-                        gi[pos] = id;
-                        gs[pos] = L * LEAF_CAP + j;
-                        if (gcnt < k) ++gcnt;
-                        if (gcnt == k) {
-                            worst = gd[k - 1];
-                            worst_id = gi[k - 1];
-                        }
-                        continue;
-                    }
-                    float cd = d;
-                    int cid = id, cs = L * LEAF_CAP + j;
+                if (!(w & F_DEL)) {
+                    d = sq_dist(qx, qy, qz, p.x, p.y, p.z);
+                    id = (int)(w & ID_MASK);
+                    sl = L * LEAF_CAP + j;
+                }
+            }
+            if (G == 1) {
+                if (sl >= 0) offer(d, id, sl);
+            } else {
 #pragma unroll
-                    for (int m = 0; m < KR; ++m) {
-                        const bool sw = cand_less(cd, cid, bd[m], bi[m]);
-                        const float td = bd[m];
-                        const int ti = bi[m], ts = bsl[m];
-                        bd[m] = sw ? cd : td;
-                        bi[m] = sw ? cid : ti;
-                        bsl[m] = sw ? cs : ts;
-                        cd = sw ? td : cd;
-                        cid = sw ? ti : cid;
-                        cs = sw ? ts : cs;
-                    }
-#pragma unroll
-                    for (int m = 0; m < KR; ++m)
-                        if (m == k - 1) {
-                            worst = bd[m];
-                            worst_id = bi[m];
-                        }
+                for (int s = 0; s < G; ++s) {
+                    const int src = (lane & ~(G - 1)) + s;
+                    const float ds = __shfl_sync(gmask, d, src);
+                    const int is = __shfl_sync(gmask, id, src);
+                    const int ss = __shfl_sync(gmask, sl, src);
+                    if (ss >= 0) offer(ds, is, ss);
                 }
             }
         }
-        // Pop the next subtree that can still hold a result.
-        bool found = false;
-        const float lim = fminf(max_sq, worst);
-        while (sp > 0) {
-            --sp;
-            if (st_d[sp] <= lim) {
-                cur = st_code[sp];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
+        pop();
     }
+    if (!valid || sub != 0) return;
 
     if (KMAX == 0) {
         for (int j = 0; j < k; ++j) {
@@ -311,18 +365,84 @@ inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) /
 
 template <int KMAX>
 void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
-                float* out_d2, float* out_xyz, int* out_cnt, int* slots, cudaStream_t s) {
-    knn_kernel<KMAX><<<blocks_for(nq, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz,
-                                                         out_cnt, slots);
+                float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s) {
+    if (lanes >= 4)
+        knn_kernel<KMAX, 4><<<blocks_for(nq * 4, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                    out_xyz, out_cnt, slots, perm);
+    else if (lanes == 2)
+        knn_kernel<KMAX, 2><<<blocks_for(nq * 2, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                    out_xyz, out_cnt, slots, perm);
+    else
+        knn_kernel<KMAX, 1><<<blocks_for(nq, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                out_xyz, out_cnt, slots, perm);
+}
+
+// ---- query binning -----------------------------------------------------------
+// Each query descends the top QBIN_BITS levels of the tree by the split planes;
+// the left/right path, left-aligned to QBIN_BITS bits, is an in-order index of
+// a k-d cell.  A counting sort on it puts queries of the same or neighbouring
+// cells into the same warp, so the threads of a warp traverse nearly the same
+// nodes and leaves.
+__global__ void qbin_kernel(DevTree t, const float* __restrict__ q, int q_stride, long long nq, int* __restrict__ key,
+                            int* __restrict__ hist, int nbits) {
+    long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    const float p[3] = {q[qi * q_stride], q[qi * q_stride + 1], q[qi * q_stride + 2]};
+    int code = __float_as_int(__ldg(&t.node[3].x));
+    int bits = 0, depth = 0;
+    while (code > 0 && depth < nbits) {
+        const float4 f3 = __ldg(t.node + 4 * code + 3);
+        const int go = p[__float_as_int(f3.w)] < f3.z ? 0 : 1;
+        bits = (bits << 1) | go;
+        code = go ? __float_as_int(f3.y) : __float_as_int(f3.x);
+        ++depth;
+    }
+    bits <<= (nbits - depth);
+    key[qi] = bits;
+    atomicAdd(hist + bits, 1);
+}
+
+__global__ void qbin_scatter_kernel(const int* __restrict__ key, long long nq, int* __restrict__ cursor,
+                                    int* __restrict__ perm) {
+    long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    int pos = atomicAdd(cursor + key[qi], 1);
+    perm[pos] = (int)qi;
 }
 
 }  // namespace
 
+size_t knn_temp_bytes(long long nq, int k) {
+    size_t b = 0;
+    if (nq >= QBIN_MIN_QUERIES) b += sizeof(int) * (2 * QBIN_BINS + 2 * nq) + scan_temp_bytes(QBIN_BINS) + 1024;
+    if (k > KNN_REG_MAX) b += sizeof(int) * nq * k + 256;
+    return b;
+}
+
 void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
-                float* out_d2, float* out_xyz, int* out_cnt, int* slots, cudaStream_t s) {
+                float* out_d2, float* out_xyz, int* out_cnt, void* temp, int lanes, int bin_bits, cudaStream_t s) {
     if (nq <= 0) return;
-#define IKDG_KNN(KM) knn_launch<KM>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, s)
-    if (k > 64)
+    char* tp = (char*)temp;
+    const int* perm = nullptr;
+    const int nbins = 1 << bin_bits;
+    if (nq >= QBIN_MIN_QUERIES && bin_bits > 0) {
+        int* hist = (int*)tp;
+        int* offs = hist + nbins;
+        int* key = offs + nbins;
+        int* pm = key + nq;
+        char* stemp = (char*)(pm + nq);
+        stemp = (char*)(((uintptr_t)stemp + 255) & ~(uintptr_t)255);
+        tp = stemp + ((scan_temp_bytes(QBIN_BINS) + 255) / 256) * 256;
+        cudaMemsetAsync(hist, 0, sizeof(int) * nbins, s);
+        qbin_kernel<<<blocks_for(nq, 256), 256, 0, s>>>(t, q, q_stride, nq, key, hist, bin_bits);
+        exclusive_scan(hist, offs, nbins, nullptr, stemp, s);
+        qbin_scatter_kernel<<<blocks_for(nq, 256), 256, 0, s>>>(key, nq, offs, pm);
+        perm = pm;
+    }
+    int* slots = k > KNN_REG_MAX ? (int*)tp : nullptr;
+#define IKDG_KNN(KM) \
+    knn_launch<KM>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm, lanes, s)
+    if (k > KNN_REG_MAX)
         IKDG_KNN(0);
     else if (k <= 1)
         IKDG_KNN(1);

@@ -144,9 +144,10 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             atomicOr(&t.st->err, ERR_LOOP);
             return;
         }
-        __threadfence();
+        __threadfence();  // release: this walker's writes into X's record
         int old = atomicAdd(&a.arrive[X], 1);
         if (old + 1 < __ldcg(&a.pend[X])) return;
+        __threadfence();  // acquire: the other children's writes are visible
         a.pend[X] = 0;
         a.arrive[X] = 0;
         NodeRec r = load_node_cg(t.node, X);

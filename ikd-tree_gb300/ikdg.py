@@ -35,6 +35,8 @@ SIGNATURES = {
     "ikdg_set_balance_criterion_param": (C.c_int, [_vp, C.c_float]),
     "ikdg_set_downsample_param": (C.c_int, [_vp, C.c_float]),
     "ikdg_set_leaf_fill": (C.c_int, [_vp, C.c_int]),
+    "ikdg_set_knn_lanes": (C.c_int, [_vp, C.c_int]),
+    "ikdg_set_knn_bin_bits": (C.c_int, [_vp, C.c_int]),
     "ikdg_build": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32]),
     "ikdg_add_points": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, C.c_int, _lp]),
     "ikdg_delete_points": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32]),
@@ -146,6 +148,12 @@ class KDTree:
     def set_leaf_fill(self, fill: int):
         self._check(self.lib.ikdg_set_leaf_fill(self.h, fill), "set_leaf_fill")
 
+    def set_knn_lanes(self, lanes: int):
+        self._check(self.lib.ikdg_set_knn_lanes(self.h, lanes), "set_knn_lanes")
+
+    def set_knn_bin_bits(self, bits: int):
+        self._check(self.lib.ikdg_set_knn_bin_bits(self.h, bits), "set_knn_bin_bits")
+
     # -- mutations -------------------------------------------------------------
     def Build(self, pts):
         a = _f32(pts, 3)
@@ -187,6 +195,14 @@ class KDTree:
         self._check(self.lib.ikdg_knn(self.h, _p(qa), nq, 3, k, float(max_dist), ids.ctypes.data_as(_ip), _p(d2),
                                       _p(xyz), cnt.ctypes.data_as(_ip)), "knn")
         return ids, d2, xyz, cnt
+
+    def knn_into(self, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int, xyz_ptr: int = 0,
+                 cnt_ptr: int = 0, stride: int = 3):
+        """ikdg_knn on caller-owned HOST buffers given as raw addresses (synchronous)."""
+        self._check(self.lib.ikdg_knn(self.h, C.cast(q_ptr, _fp), nq, stride, k, float(max_dist),
+                                      C.cast(ids_ptr, _ip), C.cast(d2_ptr, _fp),
+                                      C.cast(xyz_ptr, _fp) if xyz_ptr else None,
+                                      C.cast(cnt_ptr, _ip) if cnt_ptr else None), "knn")
 
     def Nearest_Search(self, point, k: int, max_dist: float = math.inf):
         """Single query, reference signature: returns (points[c,3], distances[c])."""

@@ -60,8 +60,14 @@ int ikdg_destroy(ikdg_tree* t);
 int ikdg_set_delete_criterion_param(ikdg_tree* t, float delete_param);
 int ikdg_set_balance_criterion_param(ikdg_tree* t, float balance_param);
 int ikdg_set_downsample_param(ikdg_tree* t, float box_length);
-/* Points per leaf bucket written by (re)builds, 4..32 (default 16). */
+/* Tuning knobs (no counterpart in the reference): points per leaf bucket
+ * written by (re)builds, 4..32 (default 16); threads cooperating on one kNN
+ * query, 1, 2 or 4 (default 1); tree levels used to sort a kNN batch into
+ * spatially coherent order before the search, 0..16 (default 16; batches
+ * under 2048 queries are never sorted). */
 int ikdg_set_leaf_fill(ikdg_tree* t, int fill);
+int ikdg_set_knn_lanes(ikdg_tree* t, int lanes);
+int ikdg_set_knn_bin_bits(ikdg_tree* t, int bits);
 
 /* Build(PointVector) (ikd_Tree.h:235, ikd_Tree.cpp:352-364). */
 int ikdg_build(ikdg_tree* t, const float* xyz, int64_t n, int32_t stride);

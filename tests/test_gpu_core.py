@@ -202,3 +202,45 @@ def test_growth_and_rebalance(ikdg_mod):
     tree.rebuild()
     assert tree.size() == tree.validnum()
     assert_knn(tree, ref, q, 10)
+
+
+def test_knn_binned_batches_match(ikdg_mod):
+    # Batches of >= 2048 queries are reordered by k-d cell before the search;
+    # results must be identical to small (unbinned) batches and the model.
+    rng = np.random.default_rng(21)
+    pts = rng.uniform(-30, 30, (200000, 3)).astype(np.float32)
+    q = rng.uniform(-31, 31, (12000, 3)).astype(np.float32)
+    tree = ikdg_mod.KDTree()
+    tree.Build(pts)
+    for k, md in ((5, np.inf), (9, 1.5), (70, np.inf)):
+        ids, d2, xyz, cnt = tree.knn(q, k, md)
+        for lo in range(0, len(q), 1000):
+            i2, d22, x2, c2 = tree.knn(q[lo:lo + 1000], k, md)
+            assert np.array_equal(ids[lo:lo + 1000], i2) and np.array_equal(d2[lo:lo + 1000], d22)
+            assert np.array_equal(xyz[lo:lo + 1000], x2) and np.array_equal(cnt[lo:lo + 1000], c2)
+    ref = spec.SpecTree()
+    ref.Build(pts)
+    sub = q[:3000]
+    ids, d2, _, _ = tree.knn(sub, 5)
+    rid, rd2 = ref.knn(sub, 5)
+    assert np.array_equal(ids, rid) and np.array_equal(d2, rd2)
+
+
+def test_host_direct_and_staged_paths_agree(ikdg_mod, monkeypatch):
+    # Where the GPU can address pageable host memory the host-pointer search
+    # runs directly on the caller's buffers; IKDG_HOST_STAGING=1 forces the
+    # copy path.  Both must give identical results.
+    rng = np.random.default_rng(31)
+    pts = rng.uniform(-10, 10, (50000, 3)).astype(np.float32)
+    q = rng.uniform(-10, 10, (30000, 3)).astype(np.float32)
+    direct = ikdg_mod.KDTree()
+    monkeypatch.setenv("IKDG_HOST_STAGING", "1")
+    staged = ikdg_mod.KDTree()
+    monkeypatch.delenv("IKDG_HOST_STAGING")
+    for t in (direct, staged):
+        t.Build(pts)
+    for k, md in ((5, np.inf), (11, 0.8)):
+        a = direct.knn(q, k, md)
+        b = staged.knn(q, k, md)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
