@@ -932,6 +932,28 @@ int ikdg_knn_device(ikdg_tree* h, const float* q, int64_t nq, int32_t stride, in
     return guarded(h, [&](ikdg::Tree& t) { t.knn(q, nq, stride, k, max_dist, ids, d2, xyz, cnt, true); });
 }
 
+int ikdg_knn_device_noalloc(ikdg_tree* h, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
+                            int32_t* ids, float* d2, float* xyz, int32_t* cnt) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        if (nq < 0 || stride < 3 || k < 1 || (nq > 0 && (q == nullptr || ids == nullptr || d2 == nullptr)))
+            throw ikdg::BadArg{"knn_device_noalloc: bad arguments"};
+        if (k > ikdg::KNN_REG_MAX) throw ikdg::BadArg{"knn_device_noalloc: k must be <= 64"};
+        if (nq > ikdg::NOALLOC_MAX_QUERIES)
+            throw ikdg::BadArg{"knn_device_noalloc: at most " + std::to_string(ikdg::NOALLOC_MAX_QUERIES) +
+                               " queries per call (size of the static scratch array)"};
+        if (nq == 0) return;
+        void* scratch = nullptr;
+        CK(ikdg::noalloc_scratch(t.device, &scratch));
+        if (ikdg::knn_temp_bytes(nq, k) > ikdg::noalloc_scratch_bytes())
+            throw ikdg::Internal{"knn_device_noalloc: scratch array too small"};
+        // Always sorts the batch (bins at QBIN_BITS levels): the sort is the
+        // part that needs scratch.  Nothing here allocates.
+        ikdg::launch_knn(t.dt, q, stride, nq, k, ikdg::max_sq_threshold(max_dist), ids, d2, xyz, cnt, scratch,
+                         t.knn_lanes, ikdg::QBIN_BITS, t.stream);
+        CK(cudaGetLastError());
+    });
+}
+
 int ikdg_box_search(ikdg_tree* h, const float* boxes, int64_t nb, int64_t* offsets, int32_t* ids, float* xyz,
                     int64_t capacity, int64_t* total) {
     return guarded(h, [&](ikdg::Tree& t) {

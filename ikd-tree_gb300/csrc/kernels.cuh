@@ -55,6 +55,11 @@ constexpr int QBIN_BITS = 16;
 constexpr int QBIN_BINS = 1 << QBIN_BITS;
 constexpr long long QBIN_MIN_QUERIES = 2048;
 size_t knn_temp_bytes(long long nq, int k);
+// Allocation-free kNN: limit on the batch size and the device address of the
+// shared scratch array (looked up on the first call per device).
+constexpr long long NOALLOC_MAX_QUERIES = 1 << 18;
+cudaError_t noalloc_scratch(int device, void** ptr);
+size_t noalloc_scratch_bytes();
 // `lanes` (1, 2 or 4) threads cooperate on each query; `bin_bits` (0 = off,
 // at most QBIN_BITS) levels of the tree order the queries before the search.
 void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq,

@@ -14,6 +14,8 @@
 //     boundary is admitted or lost by rounding.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "kernels.cuh"
 
 namespace ikdg {
@@ -462,6 +464,39 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
         IKDG_KNN(64);
 #undef IKDG_KNN
 }
+
+// ---- kNN without allocation -----------------------------------------------------
+// Scratch of the allocation-free kNN entry point (ikdg_knn_device_noalloc): the
+// query sort's bin counters, bin offsets, per-query keys and permutation, and
+// the prefix-sum partials, for at most NOALLOC_MAX_QUERIES queries.  It is a
+// file-scope device array, so it exists on every GPU that loads the library
+// until the process exits, and every call shares it.
+constexpr size_t NOALLOC_SCRATCH_BYTES = ((size_t)(2 * QBIN_BINS + 2 * NOALLOC_MAX_QUERIES) * sizeof(int) + 4096 +
+                                          64 * 1024);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+}  // namespace
+
+// Device address of the scratch array on the current device.  Looked up once
+// per device (the first call on a device does this set-up, which is why that
+// first call must not happen inside a stream capture); later calls reuse it.
+cudaError_t noalloc_scratch(int device, void** ptr) {
+    if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[device] == nullptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[device] = p;
+    }
+    *ptr = g_noalloc_ptr[device];
+    return cudaSuccess;
+}
+
+size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_BYTES; }
 
 void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius, long long nq,
                   long long* counts, const long long* offsets, int* ids, float* xyz, cudaStream_t s) {

@@ -44,6 +44,8 @@ SIGNATURES = {
     "ikdg_add_boxes": (C.c_int, [_vp, _fp, C.c_int64]),
     "ikdg_knn": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _ip, _fp, _fp, _ip]),
     "ikdg_knn_device": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _vp, _vp, _vp, _vp]),
+    "ikdg_knn_device_noalloc": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _vp, _vp, _vp,
+                                          _vp]),
     "ikdg_box_search": (C.c_int, [_vp, _fp, C.c_int64, _lp, _ip, _fp, C.c_int64, _lp]),
     "ikdg_radius_search": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, _fp, C.c_int32, _lp, _ip, _fp, C.c_int64,
                                      _lp]),
@@ -312,6 +314,13 @@ class KDTree:
 
     def synchronize(self):
         self._check(self.lib.ikdg_synchronize(self.h), "synchronize")
+
+    def knn_device_noalloc(self, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int,
+                           xyz_ptr: int = 0, cnt_ptr: int = 0, stride: int = 3):
+        """kNN on device buffers that allocates no device memory (see ikdg.h)."""
+        self._check(self.lib.ikdg_knn_device_noalloc(self.h, _vp(q_ptr), nq, stride, k, float(max_dist),
+                                                     _vp(ids_ptr), _vp(d2_ptr), _vp(xyz_ptr or None),
+                                                     _vp(cnt_ptr or None)), "knn_device_noalloc")
 
     def knn_device(self, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int,
                    xyz_ptr: int = 0, cnt_ptr: int = 0, stride: int = 3):

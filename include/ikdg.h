@@ -105,6 +105,24 @@ int ikdg_knn(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k
 int ikdg_knn_device(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
                     int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
 
+/* kNN for callers that cannot allocate device memory (no counterpart in the
+ * reference).  Code that runs where cudaMalloc is off limits - inside a CUDA
+ * graph capture region, in a real-time loop that must not hit the allocator,
+ * or beside a framework that owns all device memory - can still search the
+ * tree: this variant of ikdg_knn_device calls no cudaMalloc / cudaFree and no
+ * allocating library routine.  It always sorts the batch into spatially
+ * coherent order, and the sort's scratch lives in one static device array of
+ * the library (about 2.7 MB, held on every GPU that loads libikdg until the
+ * process exits).  Limits: nq <= 262144 queries and k <= 64 per call; larger
+ * requests fail with IKDG_BAD_ARG.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array: calls that can overlap on the GPU (for
+ * example on two trees with different streams) race on it and must be
+ * serialised by the caller.  Pointers are device pointers; asynchronous on
+ * the tree's stream; results equal ikdg_knn_device's. */
+int ikdg_knn_device_noalloc(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
+                            int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
+
 /* Box_Search(const BoxPointType&, PointVector&) (ikd_Tree.h:237,
  * ikd_Tree.cpp:399-404), batched over nb boxes.  Results are CSR: hits of box
  * i are ids[offsets[i] .. offsets[i+1]) (and xyz, 3 floats each, may be NULL).
