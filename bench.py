@@ -11,8 +11,12 @@ against a 1M-point map (uniform in [-50, 50]^3, float32, seeded synthetic data).
            ids + squared distances + points out, copies included.
   roofline - the kNN kernel against the measured HBM copy bandwidth, with the
            algorithmic bytes per query 12 + 8k + 16*32 + 32*ceil(log2(N/32)).
-  update_ms_per_scan - Add_Points(20k points, 0.5 m voxel downsampling) plus a
-           Delete_Point_Boxes call, per simulated scan, through the host API.
+  update_ms_per_scan - LiDAR-like incremental mapping: a 2M-point map (ground
+           plane + 200 walls), ray-cast 32x625 scans along a 1 m/scan walk;
+           per scan Add_Points with 0.5 m voxel downsampling plus
+           Delete_Point_Boxes keeping a 200 m cube around the pose, through
+           the host API (median over the scans after the first; the first
+           scan's deletion removes most of the map and is reported apart).
   cpu_baseline - the CPU restatement of the reference (oracle port) on this
            host's cores, same map and queries.
 
@@ -44,7 +48,6 @@ N_Q = 100_000
 K = 5
 EXTENT = 50.0
 MAP_SEED = 1002
-SCAN_POINTS = 20_000
 DS = 0.5
 WORKLOAD = "knn_k5_map1M_uniform_q100k"
 METRIC = "kNN queries/sec (k=5, 1M map)"
@@ -63,14 +66,37 @@ def make_queries(step: int) -> np.ndarray:
     return np.random.default_rng(7000 + step).uniform(-EXTENT, EXTENT, (N_Q, 3)).astype(np.float32)
 
 
-def make_scan(step: int):
-    """A 20k-point scan around a pose moving 1 m per scan, plus one delete box."""
-    rng = np.random.default_rng(9000 + step)
-    pose = np.array([-30.0 + step, 0.0, 0.0])
-    pts = (pose + rng.uniform(-20, 20, (SCAN_POINTS, 3))).astype(np.float32)
-    c = rng.uniform(-EXTENT, EXTENT, 3)
-    box = np.concatenate([c - 2.5, c + 2.5]).astype(np.float32).reshape(1, 6)
-    return pts, box
+LIDAR_MAP = 2_000_000
+LIDAR_SCANS = 12
+
+
+def lidar_workload():
+    """The LiDAR-like mapping stream: base map, then per scan (points, boxes)."""
+    import synthetic as S
+    world = S.lidar_world(2001)
+    base = S.lidar_map(world, LIDAR_MAP, 2002)
+    scans = []
+    for s, pose in enumerate(S.trajectory(LIDAR_SCANS, 2003)):
+        pts = S.lidar_scan(world, pose, 5000 + s)
+        scans.append((pts, S.cube_complement_boxes((pose[0], pose[1], 1.8), 100.0)))
+    return base, scans
+
+
+def run_scans(tree, scans, knn):
+    """Per scan: kNN of the scan (k=5, 5 m), then the timed map update."""
+    knn_ms, upd_ms = [], []
+    for pts, boxes in scans:
+        t0 = time.perf_counter()
+        knn(pts)
+        t1 = time.perf_counter()
+        tree.Add_Points(pts, True)
+        tree.Delete_Point_Boxes(boxes)
+        t2 = time.perf_counter()
+        knn_ms.append(1e3 * (t1 - t0))
+        upd_ms.append(1e3 * (t2 - t1))
+    return {"update_ms_per_scan": statistics.median(upd_ms[1:]), "update_ms_first_scan": upd_ms[0],
+            "scan_knn_ms": statistics.median(knn_ms[1:]),
+            "scan_points": int(statistics.median([len(p) for p, _ in scans]))}
 
 
 def dist_env():
@@ -155,19 +181,19 @@ def cpu_baseline(pts, queries, steps: int):
         t0 = time.perf_counter()
         t.knn(queries[s % len(queries)], K, nthreads=cores)
         times.append(time.perf_counter() - t0)
-    # Scan update on one core (mutations are single-caller in the reference).
-    upd = []
-    for s in range(3):
-        scan, box = make_scan(s)
-        t0 = time.perf_counter()
-        t.Add_Points(scan, True)
-        t.Delete_Point_Boxes(box)
-        upd.append(time.perf_counter() - t0)
     t.close()
     qps = N_Q / statistics.median(times)
+    # LiDAR mapping stream: kNN over all cores, mutations on one caller (the
+    # reference's mutations are single-caller).
+    base, scans = lidar_workload()
+    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind="port")
+    t.Build(base)
+    upd = run_scans(t, scans, lambda p: t.knn(p, K, 5.0, nthreads=cores))
+    t.close()
     return {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries",
-            "update_ms_per_scan": 1e3 * statistics.median(upd)}
+            "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries; "
+                      f"{LIDAR_SCANS} LiDAR scans on the {LIDAR_MAP}-point map",
+            **upd}
 
 
 def run_reference(args):
@@ -188,7 +214,8 @@ def run_reference(args):
         "cpu_baseline": {"value": cb["value"], "unit": "queries/s", "cores": cb["cores"], "kind": cb["kind"],
                          "sample": cb["sample"]},
         "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "update_ms_per_scan": cb["update_ms_per_scan"],
+        "update_ms_per_scan": cb["update_ms_per_scan"], "update_ms_first_scan": cb["update_ms_first_scan"],
+        "scan_knn_ms": cb["scan_knn_ms"],
     }
     print(json.dumps(line), flush=True)
 
@@ -275,14 +302,12 @@ def run_ours(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_step = statistics.mean(e2e_ms)
 
-    # ---- per-scan update latency (host API, synchronous)
-    upd = []
-    for s in range(max(3, min(Kst, 10))):
-        scan, box = make_scan(s)
-        t0 = time.perf_counter()
-        tree.Add_Points(scan, True)
-        tree.Delete_Point_Boxes(box)
-        upd.append(1e3 * (time.perf_counter() - t0))
+    # ---- LiDAR mapping stream (host API, synchronous)
+    base, scans = lidar_workload()
+    lt = ikdg.KDTree(0.5, 0.6, DS, device=local)
+    lt.Build(base)
+    lidar = run_scans(lt, scans, lambda p: lt.knn(p, K, 5.0, want_xyz=True))
+    lt.close()
 
     # ---- aggregate over ranks (max time, summed throughput)
     if world > 1:
@@ -307,7 +332,9 @@ def run_ours(args):
                      "bytes_per_query": bytes_per_query(N_MAP, K)},
         "clocks": clocks,
         "gpu_launches": 2 * Kst,
-        "update_ms_per_scan": statistics.median(upd),
+        "update_ms_per_scan": lidar["update_ms_per_scan"],
+        "update": {"workload": f"lidar map {LIDAR_MAP} pts, {LIDAR_SCANS} scans of ~{lidar['scan_points']} pts, "
+                               "0.5 m downsampling, 200 m sliding cube", **lidar},
         "wall_s_timed_region": t_wall,
     }
     if rank == 0 and world == 1 and not args.no_cpu:

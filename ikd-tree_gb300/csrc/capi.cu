@@ -94,6 +94,50 @@ float max_sq_threshold(double max_dist) {
     return f;
 }
 
+// SO(3) exponential (Rodrigues) and its right Jacobian, in double.
+void so3_exp(const double w[3], double R[9]) {
+    const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    double a, b;  // R = I + a [w]x + b [w]x^2
+    if (th < 1e-6) {
+        a = 1.0 - th * th / 6.0;
+        b = 0.5 - th * th / 24.0;
+    } else {
+        a = std::sin(th) / th;
+        b = (1.0 - std::cos(th)) / (th * th);
+    }
+    const double K[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+    double K2[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            double s = 0;
+            for (int m = 0; m < 3; ++m) s += K[3 * r + m] * K[3 * m + c];
+            K2[3 * r + c] = s;
+        }
+    for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0 ? 1.0 : 0.0) + a * K[i] + b * K2[i];
+}
+
+// Right Jacobian J_r(w) = I - (1 - cos t)/t^2 [w]x + (t - sin t)/t^3 [w]x^2.
+void so3_jr(const double w[3], double J[9]) {
+    const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    double a, b;
+    if (th < 1e-4) {
+        a = 0.5 - th * th / 24.0;
+        b = 1.0 / 6.0 - th * th / 120.0;
+    } else {
+        a = (1.0 - std::cos(th)) / (th * th);
+        b = (th - std::sin(th)) / (th * th * th);
+    }
+    const double K[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+    double K2[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            double s = 0;
+            for (int m = 0; m < 3; ++m) s += K[3 * r + m] * K[3 * m + c];
+            K2[3 * r + c] = s;
+        }
+    for (int i = 0; i < 9; ++i) J[i] = (i % 4 == 0 ? 1.0 : 0.0) - a * K[i] + b * K2[i];
+}
+
 template <class T>
 void grow_array(T*& p, size_t old_n, size_t new_n, int fill_byte, cudaStream_t s) {
     T* q = nullptr;
@@ -672,6 +716,79 @@ struct Tree {
         read_status();
     }
 
+    // ---- point-to-plane registration (no counterpart in the reference) -----------
+    void upload_pose(const double pose[6], double* Rt_dev) {
+        double R[9];
+        so3_exp(pose, R);
+        double h[12];
+        for (int i = 0; i < 9; ++i) h[i] = R[i];
+        for (int i = 0; i < 3; ++i) h[9 + i] = pose[3 + i];
+        CK(cudaMemcpyAsync(Rt_dev, h, sizeof(h), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));  // h lives on this stack frame
+    }
+
+    void p2p_forward(const float* scan, long long n, const double* pose, int k, double max_dist, float thresh,
+                     float* planes, float* res, int* valid, double* loss) {
+        if (n < 0 || scan == nullptr || pose == nullptr || planes == nullptr || res == nullptr || valid == nullptr ||
+            k < 3 || k > KNN_REG_MAX)
+            throw BadArg{"p2p_forward: bad arguments"};
+        if (loss) *loss = 0;
+        if (n == 0) return;
+        reset_counters();
+        const int nb = reg_blocks(n);
+        op.ensure(align_up(sizeof(double) * 12) + align_up(sizeof(float) * 3 * n) + align_up(sizeof(int) * n * k) +
+                      align_up(sizeof(float) * n * k) + align_up(sizeof(float) * 3 * n * k) + align_up(sizeof(int) * n) +
+                      align_up(sizeof(double) * nb) + align_up(knn_temp_bytes(n, k)),
+                  stream);
+        Carver c(op.p);
+        double* Rt = c.take<double>(12);
+        float* w = c.take<float>(3 * n);
+        int* ids = c.take<int>((size_t)n * k);
+        float* d2 = c.take<float>((size_t)n * k);
+        float* nbr = c.take<float>((size_t)3 * n * k);
+        int* cnt = c.take<int>(n);
+        double* part = c.take<double>(nb);
+        char* temp = c.take<char>(knn_temp_bytes(n, k));
+        upload_pose(pose, Rt);
+        launch_transform(scan, n, Rt, w, stream);
+        launch_knn(dt, w, 3, n, k, max_sq_threshold(max_dist), ids, d2, nbr, cnt, temp, knn_lanes, knn_bin_bits,
+                   stream);
+        launch_plane_residual(scan, Rt, n, k, nbr, cnt, thresh, (float4*)planes, res, valid, part, stream);
+        std::vector<double> h(nb);
+        CK(cudaMemcpyAsync(h.data(), part, sizeof(double) * nb, cudaMemcpyDeviceToHost, stream));
+        read_status();
+        double s = 0;
+        for (double v : h) s += v;
+        if (loss) *loss = s;
+    }
+
+    void p2p_adjoint(const float* scan, long long n, const double* pose, const float* planes, const float* res,
+                     const int* valid, double grad_loss, float* grad_points, double* grad_pose) {
+        if (n < 0 || scan == nullptr || pose == nullptr || planes == nullptr || res == nullptr || valid == nullptr ||
+            grad_pose == nullptr)
+            throw BadArg{"p2p_adjoint: bad arguments"};
+        for (int i = 0; i < 6; ++i) grad_pose[i] = 0;
+        if (n == 0) return;
+        const int nb = reg_blocks(n);
+        op.ensure(align_up(sizeof(double) * 12) + align_up(sizeof(double) * 6 * nb), stream);
+        Carver c(op.p);
+        double* Rt = c.take<double>(12);
+        double* part = c.take<double>((size_t)6 * nb);
+        upload_pose(pose, Rt);
+        launch_adjoint(scan, n, Rt, (const float4*)planes, res, valid, (float)grad_loss, grad_points, part, stream);
+        std::vector<double> h(6 * (size_t)nb);
+        CK(cudaMemcpyAsync(h.data(), part, sizeof(double) * 6 * nb, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        double s[6] = {0, 0, 0, 0, 0, 0};
+        for (int b = 0; b < nb; ++b)
+            for (int j = 0; j < 6; ++j) s[j] += h[6 * (size_t)b + j];
+        double J[9];
+        so3_jr(pose, J);
+        for (int r = 0; r < 3; ++r)  // dL/domega = J_r^T (sum p x R^T g)
+            grad_pose[r] = J[r] * s[3] + J[3 + r] * s[4] + J[6 + r] * s[5];
+        for (int r = 0; r < 3; ++r) grad_pose[3 + r] = s[r];
+    }
+
     void flatten(float* xyz, int* ids, long long capacity, long long* n) {
         if (n == nullptr) throw BadArg{"flatten: bad arguments"};
         long long valid = (long long)st->root_slots - st->root_deleted;
@@ -876,7 +993,7 @@ int ikdg_set_downsample_param(ikdg_tree* h, float v) {
 }
 int ikdg_set_leaf_fill(ikdg_tree* h, int fill) {
     return guarded(h, [&](ikdg::Tree& t) {
-        if (fill < 4 || fill > ikdg::LEAF_CAP) throw ikdg::BadArg{"leaf fill must be in [4, 32]"};
+        if (fill < 8 || fill > ikdg::LEAF_CAP) throw ikdg::BadArg{"leaf fill must be in [8, 32]"};
         t.fill = fill;
     });
 }
@@ -951,6 +1068,21 @@ int ikdg_knn_device_noalloc(ikdg_tree* h, const float* q, int64_t nq, int32_t st
         ikdg::launch_knn(t.dt, q, stride, nq, k, ikdg::max_sq_threshold(max_dist), ids, d2, xyz, cnt, scratch,
                          t.knn_lanes, ikdg::QBIN_BITS, t.stream);
         CK(cudaGetLastError());
+    });
+}
+
+int ikdg_p2p_forward(ikdg_tree* h, const float* scan, int64_t n, const double* pose, int32_t k, double max_dist,
+                     float plane_thresh, float* planes, float* residuals, int32_t* valid, double* loss) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        t.p2p_forward(scan, n, pose, k, max_dist, plane_thresh, planes, residuals, valid, loss);
+    });
+}
+
+int ikdg_p2p_adjoint(ikdg_tree* h, const float* scan, int64_t n, const double* pose, const float* planes,
+                     const float* residuals, const int32_t* valid, double grad_loss, float* grad_points,
+                     double* grad_pose) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        t.p2p_adjoint(scan, n, pose, planes, residuals, valid, grad_loss, grad_points, grad_pose);
     });
 }
 

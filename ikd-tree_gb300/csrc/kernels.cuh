@@ -36,7 +36,8 @@ struct BuildScratch {
     int* scan_out;       // [3 * n]
     int4* segs[2];       // 2 x [max_segs]  {s, e, link, pad}
     int4* seginfo;       // [max_segs]      {kind, axis/leaf, mid, child_base}
-    int* nseg;           // [2] device counters
+    int4* local_jobs;    // [max_segs]      {s, e, link} for the CTA-local builder
+    int* nseg;           // [4] device counters (two levels, local jobs)
     void* temp;          // scan / sort temp
 };
 size_t build_scratch_bytes(long long n, int njobs, int fill);
@@ -72,6 +73,17 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
 void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius,
                   long long nq, long long* counts, const long long* offsets, int* ids, float* xyz,
                   cudaStream_t s);
+
+// ---- register.cu ---------------------------------------------------------------
+// Rt_dev: 12 doubles, R row-major then t.  planes: 2 float4 per point ({n,d}
+// and a point c on the plane).  partial: per-block double sums (reg_blocks(n)
+// entries of 1 (loss) or 6 (adjoint) doubles).
+int reg_blocks(long long n);
+void launch_transform(const float* p, long long n, const double* Rt_dev, float* w, cudaStream_t s);
+void launch_plane_residual(const float* p, const double* Rt_dev, long long n, int k, const float* nb, const int* cnt,
+                           float thresh, float4* planes, float* res, int* valid, double* partial, cudaStream_t s);
+void launch_adjoint(const float* p, long long n, const double* Rt_dev, const float4* planes, const float* res,
+                    const int* valid, float dl, float* grad_p, double* partial, cudaStream_t s);
 
 // ---- update.cu --------------------------------------------------------------
 struct UpdateScratch;

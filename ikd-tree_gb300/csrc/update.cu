@@ -719,7 +719,9 @@ __global__ void snapshot_root_kernel(DevTree t) {
 // boxes of neighbouring voxels overlap or leave gaps by one ulp).  Such points
 // are detected and processed alone, in input order, which keeps the result
 // identical to the sequential loop.  Among points of S at the same distance
-// the smaller id wins (the reference takes the first in traversal order).
+// the smaller id wins (the reference takes the first in traversal order).  A
+// winner that was already in the map is re-inserted under its own id; a new
+// point i of the batch gets id first_id + i.
 
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     h ^= h >> 16;
@@ -900,6 +902,8 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
     bool s_is_s0 = true, del_s0 = false, have_ins = false;
     float cx = 0.f, cy = 0.f, cz = 0.f, cd = 0.f;
     long long ins_idx = -1;
+    int ins_old_id = -1;  // the winner is an existing point: it keeps its id
+    int cw_old = -1;
     int triggers = 0;
     for (long long jj = j; jj < n && d.hkey[0][jj] == h; ++jj) {
         uint32_t idx = d.hval[0][jj];
@@ -908,10 +912,12 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
         float4 p = d.pts[idx];
         float pd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
         float wx = p.x, wy = p.y, wz = p.z, wd = pd;
+        int w_old = -1;
         bool trig;
         if (s_is_s0) {
             if (n0 > 0 && best.w < pd) {
                 wx = best.x; wy = best.y; wz = best.z; wd = best.w;
+                w_old = info.z;
             }
             trig = n0 > 1 || same_point(p.x, p.y, p.z, wx, wy, wz);
             if (trig) {
@@ -921,20 +927,23 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
         } else {
             if (cd < pd) {
                 wx = cx; wy = cy; wz = cz; wd = cd;
+                w_old = cw_old;
             }
             trig = same_point(p.x, p.y, p.z, wx, wy, wz);
         }
         if (trig) {
             ++triggers;
             cx = wx; cy = wy; cz = wz; cd = wd;
+            cw_old = w_old;
             have_ins = true;
             ins_idx = idx;
+            ins_old_id = w_old;
         }
     }
     d.g_out[g] = make_int4(del_s0 ? 1 : 0, have_ins ? 1 : 0, triggers, 0);
     if (triggers) atomicAdd((unsigned long long*)&t.st->count2, (unsigned long long)triggers);
     if (have_ins) {
-        long long id = first_id + ins_idx;
+        long long id = ins_old_id >= 0 ? (long long)ins_old_id : first_id + ins_idx;
         if (id > MAX_ID) {
             atomicOr(&t.st->err, ERR_ID);
             return;

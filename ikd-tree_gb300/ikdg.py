@@ -49,6 +49,10 @@ SIGNATURES = {
     "ikdg_box_search": (C.c_int, [_vp, _fp, C.c_int64, _lp, _ip, _fp, C.c_int64, _lp]),
     "ikdg_radius_search": (C.c_int, [_vp, _fp, C.c_int64, C.c_int32, _fp, C.c_int32, _lp, _ip, _fp, C.c_int64,
                                      _lp]),
+    "ikdg_p2p_forward": (C.c_int, [_vp, _vp, C.c_int64, C.POINTER(C.c_double), C.c_int32, C.c_double, C.c_float,
+                                   _vp, _vp, _vp, C.POINTER(C.c_double)]),
+    "ikdg_p2p_adjoint": (C.c_int, [_vp, _vp, C.c_int64, C.POINTER(C.c_double), _vp, _vp, _vp, C.c_double, _vp,
+                                   C.POINTER(C.c_double)]),
     "ikdg_size": (C.c_int, [_vp, _lp]),
     "ikdg_validnum": (C.c_int, [_vp, _lp]),
     "ikdg_tree_range": (C.c_int, [_vp, _fp]),
@@ -314,6 +318,26 @@ class KDTree:
 
     def synchronize(self):
         self._check(self.lib.ikdg_synchronize(self.h), "synchronize")
+
+    def p2p_forward(self, scan_ptr: int, n: int, pose, k: int, max_dist: float, plane_thresh: float,
+                    planes_ptr: int, res_ptr: int, valid_ptr: int) -> float:
+        """Point-to-plane residuals on device buffers; returns the loss."""
+        pz = (C.c_double * 6)(*[float(v) for v in pose])
+        loss = C.c_double(0)
+        self._check(self.lib.ikdg_p2p_forward(self.h, _vp(scan_ptr), n, pz, k, float(max_dist), float(plane_thresh),
+                                              _vp(planes_ptr), _vp(res_ptr), _vp(valid_ptr), C.byref(loss)),
+                    "p2p_forward")
+        return loss.value
+
+    def p2p_adjoint(self, scan_ptr: int, n: int, pose, planes_ptr: int, res_ptr: int, valid_ptr: int,
+                    grad_loss: float, grad_points_ptr: int = 0):
+        """Adjoint of p2p_forward; returns dL/d(omega, t) (6 floats)."""
+        pz = (C.c_double * 6)(*[float(v) for v in pose])
+        g = (C.c_double * 6)()
+        self._check(self.lib.ikdg_p2p_adjoint(self.h, _vp(scan_ptr), n, pz, _vp(planes_ptr), _vp(res_ptr),
+                                              _vp(valid_ptr), float(grad_loss), _vp(grad_points_ptr or None), g),
+                    "p2p_adjoint")
+        return list(g)
 
     def knn_device_noalloc(self, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int,
                            xyz_ptr: int = 0, cnt_ptr: int = 0, stride: int = 3):

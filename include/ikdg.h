@@ -61,7 +61,7 @@ int ikdg_set_delete_criterion_param(ikdg_tree* t, float delete_param);
 int ikdg_set_balance_criterion_param(ikdg_tree* t, float balance_param);
 int ikdg_set_downsample_param(ikdg_tree* t, float box_length);
 /* Tuning knobs (no counterpart in the reference): points per leaf bucket
- * written by (re)builds, 4..32 (default 16); threads cooperating on one kNN
+ * written by (re)builds, 8..32 (default 16); threads cooperating on one kNN
  * query, 1, 2 or 4 (default 1); tree levels used to sort a kNN batch into
  * spatially coherent order before the search, 0..16 (default 16; batches
  * under 2048 queries are never sorted). */
@@ -137,6 +137,23 @@ int ikdg_box_search(ikdg_tree* t, const float* boxes, int64_t nb, int64_t* offse
 int ikdg_radius_search(ikdg_tree* t, const float* centers, int64_t nq, int32_t stride, const float* radius,
                        int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
                        int64_t* total);
+
+/* Scan-to-map point-to-plane residuals on top of Nearest_Search (no
+ * counterpart in the reference; the step its main consumer, FAST-LIO2, runs on
+ * every kNN result).  Device pointers except pose / loss / grad_pose (host).
+ * pose = {omega_x, omega_y, omega_z, t_x, t_y, t_z}: w_i = Exp(omega) p_i + t.
+ * Forward: kNN (k, max_dist) of every w_i; least-squares plane n.q + d = 0
+ * through the k neighbours (A x = -1, n = x/|x|, d = 1/|x|), valid when every
+ * neighbour lies within plane_thresh; planes[8i..8i+7] = {n, d, c, 0} with c
+ * a point on the plane; r_i = n.(w_i - c) (= n.w_i + d); *loss = 1/2 sum
+ * over valid points of r_i^2.
+ * Adjoint (neighbours and planes held fixed): grad_points[i] = dL/dp_i (may
+ * be NULL) and grad_pose = dL/d(omega, t), scaled by grad_loss. */
+int ikdg_p2p_forward(ikdg_tree* t, const float* scan, int64_t n, const double* pose, int32_t k, double max_dist,
+                     float plane_thresh, float* planes, float* residuals, int32_t* valid, double* loss);
+int ikdg_p2p_adjoint(ikdg_tree* t, const float* scan, int64_t n, const double* pose, const float* planes,
+                     const float* residuals, const int32_t* valid, double grad_loss, float* grad_points,
+                     double* grad_pose);
 
 /* size() (ikd_Tree.cpp:78-96): stored points, deleted ones not yet dropped by a
  * rebuild included.  validnum() (ikd_Tree.cpp:128-145): valid points. */

@@ -18,7 +18,8 @@ so results are independent of tree shape:
 
 Point ids follow the library: Build numbers points 0..n-1; a later call with
 m points reserves ids next_id .. next_id+m-1, and the point inserted for input
-i gets id next_id + i.
+i gets id next_id + i.  A downsampling winner that was already in the map is
+re-inserted under its own id.
 """
 from __future__ import annotations
 
@@ -90,15 +91,17 @@ class SpecTree:
             inside = inside[np.argsort(self.ids[inside], kind="stable")]
             best_d = sq_dist(p[i], mid)
             winner = p[i]
+            winner_id = first + i
             for j in inside:
                 d = sq_dist(self.pts[j], mid)
                 if d < best_d:
                     best_d = d
                     winner = self.pts[j]
+                    winner_id = int(self.ids[j])
             if len(inside) > 1 or same_point(p[i], winner):
                 winner = np.array(winner, F32)
                 self.valid[inside] = False
-                self._append(winner, first + i)
+                self._append(winner, winner_id)
                 count += 1
         return count
 
