@@ -19,6 +19,16 @@ against a 1M-point map (uniform in [-50, 50]^3, float32, seeded synthetic data).
            scan's deletion removes most of the map and is reported apart).
   cpu_baseline - the CPU restatement of the reference (oracle port) on this
            host's cores, same map and queries.
+  stress - a 20M-point map (uniform slab plus planar clusters): device kNN of
+           1M queries at k in {1, 5, 16, 32} (max 2 m) with the achieved
+           fraction of the HBM roofline, radius search r = 1 m, 1000 box
+           deletions (1-20 m sides), then the same queries again.
+  batched - 64 independent maps (10k-1M points each, 14.7M in all) with
+           log-uniform query batches (1.37M queries: 60 % kNN k 1-16, 20 %
+           box, 20 % radius), all on device buffers: the plain per-call
+           device path (one ikdg_*_device call per request) against one
+           graph launch of a multi-tree batch, host wall clock around issue
+           and completion of each, before and after the batch autotuner.
 
 `--impl reference` times that CPU implementation alone on the same workload.
 Multi-GPU (torchrun): every rank holds its own replica of the tree (the path
@@ -166,6 +176,208 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+MM_SEED = 3001
+STRESS_N = 20_000_000
+STRESS_Q = 1_000_000
+
+
+def stress_bench(ikdg, torch, device: int, reps: int = 3) -> dict:
+    """Scale stress: 20M-point map, 1M-query batches, 1000 box deletions."""
+    import synthetic as S
+    dev = torch.device("cuda", device)
+    pts = S.stress_map(STRESS_N, 5005)
+    rng = np.random.default_rng(5006)
+    qh = np.empty((STRESS_Q, 3), np.float32)
+    qh[:, :2] = rng.uniform(-500, 500, (STRESS_Q, 2))
+    qh[:, 2] = rng.uniform(0, 50, STRESS_Q)
+    tree = ikdg.KDTree(0.5, 0.6, DS, device=device)
+    t0 = time.perf_counter()
+    tree.Build(pts)
+    build_ms = 1e3 * (time.perf_counter() - t0)
+    st = torch.cuda.ExternalStream(tree.stream(), device=dev)
+    q = torch.from_numpy(qh).to(dev)
+    kmax = 32
+    ids = torch.empty((STRESS_Q, kmax), dtype=torch.int32, device=dev)
+    d2 = torch.empty((STRESS_Q, kmax), dtype=torch.float32, device=dev)
+    xyz = torch.empty((STRESS_Q, kmax, 3), dtype=torch.float32, device=dev)
+    cnt = torch.empty((STRESS_Q,), dtype=torch.int32, device=dev)
+    offs = torch.empty((STRESS_Q + 1,), dtype=torch.int64, device=dev)
+    total = torch.zeros((1,), dtype=torch.int64, device=dev)
+    radius = torch.full((STRESS_Q,), 1.0, dtype=torch.float32, device=dev)
+    peak, _ = measured_peak()
+
+    def ev_time(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            tree.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    def queries():
+        out = {}
+        for k in (1, 5, 16, 32):
+            ms = ev_time(lambda: tree.knn_device(q.data_ptr(), STRESS_Q, k, 2.0, ids.data_ptr(), d2.data_ptr(),
+                                                 xyz.data_ptr(), cnt.data_ptr()))
+            gbs = STRESS_Q * bytes_per_query(tree.validnum(), k) / (ms / 1e3) / 1e9
+            out[f"knn_k{k}"] = {"ms": ms, "queries_per_s": STRESS_Q / (ms / 1e3), "achieved_gbs": gbs,
+                                "hbm_frac": gbs / peak,
+                                "mean_count": float(cnt.float().mean().item())}
+        tree.radius_search_device(q.data_ptr(), STRESS_Q, radius.data_ptr(), offs.data_ptr(), 0, 0, 0,
+                                  total.data_ptr())
+        tree.synchronize()
+        cap = int(total.item())
+        rid = torch.empty((max(cap, 1),), dtype=torch.int32, device=dev)
+        rxyz = torch.empty((max(cap, 1), 3), dtype=torch.float32, device=dev)
+        ms = ev_time(lambda: tree.radius_search_device(q.data_ptr(), STRESS_Q, radius.data_ptr(), offs.data_ptr(),
+                                                       rid.data_ptr(), cap, rxyz.data_ptr(), total.data_ptr()))
+        out["radius_r1"] = {"ms": ms, "queries_per_s": STRESS_Q / (ms / 1e3), "hits": cap}
+        return out
+
+    before = queries()
+    boxes = S.random_boxes(1000, 5007)
+    t0 = time.perf_counter()
+    n_del = tree.Delete_Point_Boxes(boxes)
+    del_ms = 1e3 * (time.perf_counter() - t0)
+    after = queries()
+    res = {"workload": f"{STRESS_N} points (uniform slab [-500,500]^2 x [0,50] m + planar clusters), "
+                       f"{STRESS_Q} uniform queries, k in 1/5/16/32 max 2 m, radius 1 m, 1000 boxes 1-20 m",
+           "build_ms": build_ms, "before": before, "delete_1000_boxes_ms": del_ms, "deleted": n_del,
+           "after": after, "timing": f"CUDA events on the tree stream, median of {reps}; inputs > L2"}
+    tree.close()
+    return res
+
+
+def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -> dict:
+    """Plain per-call device path vs one graph launch of a multi-tree batch."""
+    import synthetic as S
+    dev = torch.device("cuda", device)
+    maps = S.multi_maps(MM_SEED)
+    trees, reqs = [], []
+    for m in maps:
+        t = ikdg.KDTree(0.5, 0.6, DS, device=device)
+        t.Build(m.points)
+        trees.append(t)
+
+    def zeros(shape, dt):
+        return torch.empty(shape, dtype=dt, device=dev)
+
+    n_queries = 0
+    for m, t in zip(maps, trees):
+        nk, nb, nr = len(m.knn_q), len(m.boxes), len(m.radius_q)
+        n_queries += nk + nb + nr
+        reqs.append(("knn", t, dict(q=torch.from_numpy(m.knn_q).to(dev), nq=nk, k=m.k, md=m.max_dist,
+                                    ids=zeros((nk, m.k), torch.int32), d2=zeros((nk, m.k), torch.float32),
+                                    xyz=zeros((nk, m.k, 3), torch.float32), cnt=zeros((nk,), torch.int32))))
+        for kind, q, n, rad in (("box", m.boxes, nb, None), ("radius", m.radius_q, nr, m.radius)):
+            r = dict(q=torch.from_numpy(q).to(dev), nq=n, offs=zeros((n + 1,), torch.int64),
+                     total=torch.zeros((1,), dtype=torch.int64, device=dev),
+                     rad=torch.from_numpy(rad).to(dev) if rad is not None else None)
+            if kind == "box":
+                t.box_search_device(r["q"].data_ptr(), n, r["offs"].data_ptr(), 0, 0, 0, r["total"].data_ptr())
+            else:
+                t.radius_search_device(r["q"].data_ptr(), n, r["rad"].data_ptr(), r["offs"].data_ptr(), 0, 0, 0,
+                                       r["total"].data_ptr())
+            t.synchronize()
+            cap = int(r["total"].item())
+            r["cap"] = cap
+            r["ids"] = zeros((max(cap, 1),), torch.int32)
+            r["xyz"] = zeros((max(cap, 1), 3), torch.float32)
+            reqs.append((kind, t, r))
+    n_hits = sum(r["cap"] for kind, _, r in reqs if kind != "knn")
+    n_range = sum(1 for kind, _, _ in reqs if kind != "knn")
+
+    def plain():
+        for kind, t, r in reqs:
+            if kind == "knn":
+                t.knn_device(r["q"].data_ptr(), r["nq"], r["k"], r["md"], r["ids"].data_ptr(), r["d2"].data_ptr(),
+                             r["xyz"].data_ptr(), r["cnt"].data_ptr())
+            elif kind == "box":
+                t.box_search_device(r["q"].data_ptr(), r["nq"], r["offs"].data_ptr(), r["ids"].data_ptr(),
+                                    r["cap"], r["xyz"].data_ptr(), r["total"].data_ptr())
+            else:
+                t.radius_search_device(r["q"].data_ptr(), r["nq"], r["rad"].data_ptr(), r["offs"].data_ptr(),
+                                       r["ids"].data_ptr(), r["cap"], r["xyz"].data_ptr(), r["total"].data_ptr())
+        for t in trees:
+            t.synchronize()
+
+    b = ikdg.Batch(device)
+    for kind, t, r in reqs:
+        if kind == "knn":
+            b.add_knn(t, r["q"].data_ptr(), r["nq"], r["k"], r["md"], r["ids"].data_ptr(), r["d2"].data_ptr(),
+                      r["xyz"].data_ptr(), r["cnt"].data_ptr())
+        elif kind == "box":
+            b.add_box_search(t, r["q"].data_ptr(), r["nq"], r["offs"].data_ptr(), r["ids"].data_ptr(), r["cap"],
+                             r["xyz"].data_ptr())
+        else:
+            b.add_radius_search(t, r["q"].data_ptr(), r["nq"], r["rad"].data_ptr(), r["offs"].data_ptr(),
+                                r["ids"].data_ptr(), r["cap"], r["xyz"].data_ptr())
+
+    def batched():
+        b.run()
+        b.synchronize(n_range)
+
+    def timed(fn):
+        fn()
+        fn()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            ts.append(1e3 * (time.perf_counter() - t0))
+        return statistics.median(ts)
+
+    def batch_device_ms():
+        st = torch.cuda.ExternalStream(b.stream, device=dev)
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            b.run()
+            e1.record(st)
+            b.synchronize(n_range)
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    plain_ms = timed(plain)
+    batch_ms = timed(batched)
+    batch_dev = batch_device_ms()
+    tuned = None
+    if tune:
+        t0 = time.perf_counter()
+        chosen = b.autotune(3)
+        tune_s = time.perf_counter() - t0
+        tuned_ms = timed(batched)
+        tuned_dev = batch_device_ms()
+        plain_tuned_ms = timed(plain)
+        tuned = {"batched_ms": tuned_ms, "batched_device_ms": tuned_dev, "plain_ms": plain_tuned_ms,
+                 "speedup_vs_plain": plain_tuned_ms / tuned_ms, "tune_s": tune_s,
+                 "fill_counts": {str(f): int((chosen[:, 0] == f).sum()) for f in sorted(set(chosen[:, 0]))},
+                 "lanes_counts": {str(l): int((chosen[:, 1] == l).sum()) for l in sorted(set(chosen[:, 1]))}}
+    out = {
+        "workload": f"{len(maps)} maps, {sum(len(m.points) for m in maps)} points, {n_queries} queries "
+                    f"(60% kNN k 1-16 max 1-10 m, 20% box 0.5-5 m, 20% radius 0.5-5 m), {n_hits} range hits, "
+                    "ids + points out; inputs larger than L2",
+        "queries": n_queries,
+        "plain_ms": plain_ms, "plain_queries_per_s": n_queries / (plain_ms / 1e3),
+        "batched_ms": batch_ms, "batched_queries_per_s": n_queries / (batch_ms / 1e3),
+        "batched_device_ms": batch_dev,
+        "speedup_vs_plain": plain_ms / batch_ms,
+        "autotuned": tuned,
+        "plain_launches": 64 + n_range * 5,
+        "timing": "host wall clock from issue to completion, median of %d runs" % reps,
+    }
+    b.close()
+    for t in trees:
+        t.close()
+    return out
+
+
 def cpu_baseline(pts, queries, steps: int):
     """The oracle port (CPU restatement of the reference) on all host cores."""
     sys.path.insert(0, ORACLE)
@@ -309,6 +521,10 @@ def run_ours(args):
     lidar = run_scans(lt, scans, lambda p: lt.knn(p, K, 5.0, want_xyz=True))
     lt.close()
 
+    # ---- batched multi-map workload, scale stress
+    batched = None if args.no_batch else multimap_bench(ikdg, torch, local)
+    stress = None if args.no_stress else stress_bench(ikdg, torch, local)
+
     # ---- aggregate over ranks (max time, summed throughput)
     if world > 1:
         t = torch.tensor([ms, e2e_step], dtype=torch.float64)
@@ -337,6 +553,10 @@ def run_ours(args):
                                "0.5 m downsampling, 200 m sliding cube", **lidar},
         "wall_s_timed_region": t_wall,
     }
+    if batched is not None:
+        line["batched"] = batched
+    if stress is not None:
+        line["stress"] = stress
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(pts, qhost[:3], 3)
     if rank == 0:
@@ -353,6 +573,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the multi-map batch leg")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 20M-point scale leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

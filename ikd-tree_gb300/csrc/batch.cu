@@ -1,0 +1,218 @@
+// Multi-tree batched searches: many kNN / box / radius requests over many
+// trees in one persistent launch per phase.  The reference has no batched
+// form; every request has the semantics of its per-call search (search.cuh).
+//
+// Work is cut into chunks of BATCH_THREADS threads; each CTA takes the next
+// chunk index from a device counter, finds the request it belongs to by a
+// binary search over the requests' first chunks, and runs that request's
+// search body on it.  So small requests of many trees fill the GPU together
+// and no launch is spent per request.  CTAs never wait on one another.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "search.cuh"
+
+namespace ikdg {
+namespace {
+
+// Last r in [lo, hi) with starts[r] <= c (starts ascending, starts[lo] <= c).
+__device__ __forceinline__ int find_req(const long long* __restrict__ starts, int lo, int hi, long long c) {
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(starts + mid) <= c)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Phase 1 for one register class: KC 0..4 are kNN requests with k <= 1, 2,
+// 4, 8, 16 (their final rows), KC = BATCH_RANGE_CLASS box and radius
+// requests (per-query hit counts in counts[cbase + qi]).  One kernel per class
+// keeps each at its own register count.
+template <int KC, int G>
+__global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTree* __restrict__ trees,
+                                                                     const BatchReq* __restrict__ reqs,
+                                                                     const long long* __restrict__ req_c1, int r0,
+                                                                     int r1, long long c_begin, long long c_end,
+                                                                     long long* __restrict__ counts,
+                                                                     unsigned long long* __restrict__ ctr) {
+    constexpr int KM = KC == 0 ? 1 : KC == 1 ? 2 : KC == 2 ? 4 : KC == 3 ? 8 : 16;
+    __shared__ long long s_chunk;
+    __shared__ int s_req;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long c = c_begin + (long long)atomicAdd(ctr, 1ull);
+            s_chunk = c;
+            s_req = c < c_end ? find_req(req_c1, r0, r1, c) : -1;
+        }
+        __syncthreads();
+        const long long c = s_chunk;
+        const int r = s_req;
+        __syncthreads();  // both are rewritten by the next iteration
+        if (c >= c_end) break;
+        const BatchReq& R = reqs[r];
+        const DevTree t = trees[R.tree];
+        if constexpr (KC < BATCH_RANGE_CLASS) {
+            const long long tid = (c - R.c1) * (BATCH_THREADS / G) + threadIdx.x / G;
+            search::knn_body<KM, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
+                                    nullptr);
+        } else {
+            // warp-collective body: every lane calls it
+            const long long qi = (c - R.c1) * BATCH_THREADS + threadIdx.x;
+            const bool valid = qi < R.nq;
+            const long long n =
+                R.kind == BATCH_BOX
+                    ? search::range_body<0, false>(t, R.q, R.q_stride, nullptr, 0, qi, valid, 0, 0, nullptr, nullptr)
+                    : search::range_body<1, false>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, valid, 0, 0,
+                                                   nullptr, nullptr);
+            if (valid) counts[R.cbase + qi] = n;
+        }
+    }
+}
+
+// Phase 2: range requests write their CSR offsets and, where the request's
+// capacity holds the query's results, the ids / points.
+__global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTree* __restrict__ trees,
+                                                                    const BatchReq* __restrict__ reqs,
+                                                                    const int* __restrict__ ridx,
+                                                                    const long long* __restrict__ req_c2, int nr,
+                                                                    long long c_end,
+                                                                    const long long* __restrict__ goff,
+                                                                    unsigned long long* __restrict__ ctr) {
+    __shared__ long long s_chunk;
+    __shared__ int s_req;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long c = (long long)atomicAdd(ctr, 1ull);
+            s_chunk = c;
+            s_req = c < c_end ? __ldg(ridx + find_req(req_c2, 0, nr, c)) : -1;
+        }
+        __syncthreads();
+        const long long c = s_chunk;
+        const int r = s_req;
+        __syncthreads();
+        if (c >= c_end) break;
+        const BatchReq& R = reqs[r];
+        const DevTree t = trees[R.tree];
+        const long long qi = (c - R.c2) * BATCH_THREADS + threadIdx.x;
+        const long long base = goff[R.cbase];
+        if (qi == 0) {
+            const long long tot = goff[R.cbase + R.nq] - base;
+            R.offsets[R.nq] = tot;
+            if (R.total != nullptr) *R.total = tot;
+        }
+        // warp-collective body: every lane calls it, lanes without work idle
+        bool go = qi < R.nq;
+        long long o = 0, n = 0;
+        if (go) {
+            o = goff[R.cbase + qi] - base;
+            n = goff[R.cbase + qi + 1] - goff[R.cbase + qi];
+            R.offsets[qi] = o;
+            if (n == 0 || R.ids == nullptr) {
+                go = false;
+            } else if (o + n > R.capacity) {
+                atomicOr(&t.st->err, ERR_OUTPUT);
+                go = false;
+            }
+        }
+        if (R.kind == BATCH_BOX)
+            search::range_body<0, true>(t, R.q, R.q_stride, nullptr, 0, qi, go, o, o + n, R.ids, R.xyz);
+        else
+            search::range_body<1, true>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, go, o, o + n, R.ids, R.xyz);
+    }
+}
+
+std::mutex g_grid_mu;
+
+int resident_grid(const void* fn) {
+    // On a failed query the grid falls back to one CTA per SM (or 1); the
+    // kernels are correct for any grid size.
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_THREADS, 0) != cudaSuccess) per_sm = 1;
+    cudaGetLastError();
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+}
+
+}  // namespace
+
+int batch_kclass(int k) { return k <= 1 ? 0 : k <= 2 ? 1 : k <= 4 ? 2 : k <= 8 ? 3 : 4; }
+
+namespace {
+
+template <int KC, int G>
+void search_variant(bool launch, int* grid, const DevTree* trees, const BatchReq* reqs, const long long* req_c1,
+                    int r0, int r1, long long c_begin, long long c_end, long long* counts, unsigned long long* ctr,
+                    unsigned g, cudaStream_t s) {
+    if (!launch) {
+        *grid = resident_grid((const void*)batch_search_kernel<KC, G>);
+        return;
+    }
+    batch_search_kernel<KC, G><<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr);
+}
+
+template <int KC>
+void search_lanes(int lanes, bool launch, int* grid, const DevTree* trees, const BatchReq* reqs,
+                  const long long* req_c1, int r0, int r1, long long c_begin, long long c_end, long long* counts,
+                  unsigned long long* ctr, unsigned g, cudaStream_t s) {
+    if (lanes >= 4)
+        search_variant<KC, 4>(launch, grid, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
+    else if (lanes == 2)
+        search_variant<KC, 2>(launch, grid, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
+    else
+        search_variant<KC, 1>(launch, grid, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
+}
+
+void search_dispatch(int kc, int lanes, bool launch, int* grid, const DevTree* trees, const BatchReq* reqs,
+                     const long long* req_c1, int r0, int r1, long long c_begin, long long c_end, long long* counts,
+                     unsigned long long* ctr, unsigned g, cudaStream_t s) {
+#define IKDG_BKC(KC) search_lanes<KC>(lanes, launch, grid, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s)
+    switch (kc) {
+        case 0: IKDG_BKC(0); break;
+        case 1: IKDG_BKC(1); break;
+        case 2: IKDG_BKC(2); break;
+        case 3: IKDG_BKC(3); break;
+        case 4: IKDG_BKC(4); break;
+        default:
+            search_variant<BATCH_RANGE_CLASS, 1>(launch, grid, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts,
+                                                 ctr, g, s);
+            break;
+    }
+#undef IKDG_BKC
+}
+
+}  // namespace
+
+int batch_search_grid(int kclass, int lanes) {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    int grid = 0;
+    search_dispatch(kclass, lanes, false, &grid, nullptr, nullptr, nullptr, 0, 0, 0, 0, nullptr, nullptr, 0, nullptr);
+    return grid;
+}
+
+int batch_write_grid() {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    return resident_grid((const void*)batch_write_kernel);
+}
+
+void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
+                         long long c_begin, long long c_end, int kclass, int lanes, long long* counts,
+                         unsigned long long* ctr, int grid, cudaStream_t s) {
+    if (c_end <= c_begin || r1 <= r0) return;
+    const long long chunks = c_end - c_begin;
+    const unsigned g = (unsigned)(chunks < grid ? chunks : grid);
+    search_dispatch(kclass, lanes, true, nullptr, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
+}
+
+void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
+                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s) {
+    if (c_end <= 0 || nr <= 0) return;
+    const unsigned g = (unsigned)(c_end < grid ? c_end : grid);
+    batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr);
+}
+
+}  // namespace ikdg

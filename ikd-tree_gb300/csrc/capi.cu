@@ -190,6 +190,7 @@ struct Tree {
     // mutation (slow; for tests and debugging).
     bool debug_validate = std::getenv("IKDG_DEBUG_VALIDATE") != nullptr;
     std::string dbg_note;
+    int dbg_round = 0;
 
     // ---- lifetime -------------------------------------------------------------
     void init(int dev) {
@@ -392,8 +393,30 @@ struct Tree {
             std::vector<int> sl(links);
             std::sort(sl.begin(), sl.end());
             for (int i = 1; i < nj; ++i)
-                if (sl[i] == sl[i - 1])
-                    throw Internal{"two rebuild jobs share the link " + std::to_string(sl[i]) + " (" + dbg_note + ")"};
+                if (sl[i] == sl[i - 1]) {
+                    std::string m = "two rebuild jobs share the link " + std::to_string(sl[i]) + " (" + dbg_note +
+                                    "); jobs with it:";
+                    for (int j = 0; j < nj; ++j)
+                        if (links[j] == sl[i]) {
+                            m += " [job " + std::to_string(j) + " code " + std::to_string(jobs[j]);
+                            int parent_link = -9, cnt = -9;
+                            if (jobs[j] < 0) {
+                                CK(cudaMemcpy(&parent_link, dt.lparent + code_leaf(jobs[j]), sizeof(int),
+                                              cudaMemcpyDeviceToHost));
+                                CK(cudaMemcpy(&cnt, dt.leaf_n + code_leaf(jobs[j]), sizeof(int),
+                                              cudaMemcpyDeviceToHost));
+                            } else {
+                                CK(cudaMemcpy(&parent_link, dt.nparent + jobs[j], sizeof(int), cudaMemcpyDeviceToHost));
+                            }
+                            m += " parent_link " + std::to_string(parent_link) + " leaf_n " + std::to_string(cnt) + "]";
+                        }
+                    float rec[16];
+                    CK(cudaMemcpy(rec, dt.node, sizeof(rec), cudaMemcpyDeviceToHost));
+                    int root = 0;
+                    std::memcpy(&root, &rec[12], sizeof(int));
+                    m += " root code " + std::to_string(root) + "; round " + std::to_string(dbg_round);
+                    throw Internal{m};
+                }
         }
         small.ensure(scan_temp_bytes(nj + 1) + 1024, stream);
         launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, nj, small.p, stream);
@@ -427,6 +450,7 @@ struct Tree {
         if (refit_first) {
             launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
             launch_clear_dirty(dt, aux, bound, stream);
+            if (debug_validate) check_valid("after the refit of a mutation", /*at_rest=*/false);
         }
         // The dirty list is consumed: the next update starts a fresh one.
         zero_fields(offsetof(DevStatus, n_items), sizeof(int));
@@ -443,6 +467,7 @@ struct Tree {
             }
             launch_select_jobs(dt, aux, nv, stream);
             read_status();
+            dbg_round = round;
             int nj = st->n_jobs;
             if (nj == 0) throw Internal{"violators without a topmost job"};
             run_jobs(nj, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
@@ -691,7 +716,7 @@ struct Tree {
             for (long long i = 0; i < nq; ++i) rr[i] = radius[i * rstride];
             CK(cudaMemcpyAsync(dr, rr.data(), sizeof(float) * nq, cudaMemcpyHostToDevice, stream));
         }
-        launch_range(dt, mode, dq, qs, dr, nq, dcounts, nullptr, nullptr, nullptr, stream);
+        launch_range(dt, mode, dq, qs, dr, 1, nq, dcounts, nullptr, nullptr, nullptr, -1, stream);
         std::vector<long long> counts(nq);
         CK(cudaMemcpyAsync(counts.data(), dcounts, sizeof(long long) * nq, cudaMemcpyDeviceToHost, stream));
         read_status();
@@ -709,11 +734,39 @@ struct Tree {
         Carver o(bld.p);
         int* dids = o.take<int>(acc);
         float* dxyz = xyz ? o.take<float>(acc * 3) : nullptr;
-        CK(cudaMemcpyAsync(doffs, offsets, sizeof(long long) * nq, cudaMemcpyHostToDevice, stream));
-        launch_range(dt, mode, dq, qs, dr, nq, nullptr, doffs, dids, dxyz, stream);
+        CK(cudaMemcpyAsync(doffs, offsets, sizeof(long long) * (nq + 1), cudaMemcpyHostToDevice, stream));
+        launch_range(dt, mode, dq, qs, dr, 1, nq, nullptr, doffs, dids, dxyz, -1, stream);
         CK(cudaMemcpyAsync(ids, dids, sizeof(int) * acc, cudaMemcpyDeviceToHost, stream));
         if (xyz) CK(cudaMemcpyAsync(xyz, dxyz, sizeof(float) * acc * 3, cudaMemcpyDeviceToHost, stream));
         read_status();
+        if (st->err & ERR_OUTPUT) throw Internal{"range search: hits differ between the count and write passes"};
+    }
+
+    // Device-pointer range search, asynchronous on the tree's stream: count
+    // pass, device prefix sum into offsets (offsets[nq] = total), write pass.
+    // A query whose results would end past `capacity` is not written.
+    void range_device(int mode, const float* q, long long nq, int stride, const float* radius, int rstride,
+                      long long* offsets, int* ids, float* xyz, long long capacity, long long* total) {
+        if (nq < 0 || offsets == nullptr || capacity < 0 || (nq > 0 && q == nullptr) ||
+            (capacity > 0 && ids == nullptr))
+            throw BadArg{"range search (device): bad arguments"};
+        if (mode == 1 && (stride < 3 || (nq > 0 && radius == nullptr) || rstride < 0))
+            throw BadArg{"radius search (device): bad arguments"};
+        const int qs = mode == 0 ? 6 : stride;
+        if (nq == 0) {
+            CK(cudaMemsetAsync(offsets, 0, sizeof(long long), stream));
+            if (total) CK(cudaMemsetAsync(total, 0, sizeof(long long), stream));
+            return;
+        }
+        small.ensure(align_up(sizeof(long long) * (nq + 1)) + align_up(scan_temp_bytes(nq + 1)) + 256, stream);
+        Carver c(small.p);
+        long long* counts = c.take<long long>(nq + 1);
+        void* temp = c.take<char>(scan_temp_bytes(nq + 1));
+        CK(cudaMemsetAsync(counts + nq, 0, sizeof(long long), stream));
+        launch_range(dt, mode, q, qs, radius, rstride, nq, counts, nullptr, nullptr, nullptr, -1, stream);
+        exclusive_scan(counts, offsets, nq + 1, total, temp, stream);
+        if (ids != nullptr) launch_range(dt, mode, q, qs, radius, rstride, nq, counts, offsets, ids, xyz, capacity, stream);
+        CK(cudaGetLastError());
     }
 
     // ---- point-to-plane registration (no counterpart in the reference) -----------
@@ -847,8 +900,8 @@ struct Tree {
         finish_update(nullptr, nullptr, 0, /*refit_first=*/false);
     }
 
-    void check_valid(const char* stage) {
-        long long bad = validate();
+    void check_valid(const char* stage, bool at_rest = true) {
+        long long bad = validate(at_rest);
         if (bad) {
             std::string m = std::string("structural validation failed at ") + stage + " (" + dbg_note + "): " +
                             std::to_string(bad) + " violations; first:";
@@ -857,9 +910,9 @@ struct Tree {
         }
     }
 
-    long long validate() {
+    long long validate(bool at_rest = true) {
         zero_fields(offsetof(DevStatus, bad), sizeof(long long));
-        launch_validate(dt, (long long*)((char*)st_dev + offsetof(DevStatus, bad)), stream);
+        launch_validate(dt, aux, at_rest, (long long*)((char*)st_dev + offsetof(DevStatus, bad)), stream);
         read_status();
         return st->bad;
     }
@@ -888,10 +941,413 @@ struct Tree {
     }
 };
 
+// ---- multi-tree batches (no counterpart in the reference) --------------------------
+// A list of search requests over several trees, run as one CUDA graph: the
+// trees' device descriptors are copied in, one persistent search kernel per
+// register class runs on its own graph branch, then (for box / radius
+// requests) a prefix sum over the hit counts and one persistent write kernel.
+struct Batch {
+    struct Req {
+        BatchReq d{};
+        Tree* tree = nullptr;
+        double max_dist = 0;
+        int lanes = 0;  // 0: the tree's kNN lanes setting
+    };
+    struct Group {
+        int kclass, lanes, r0, r1;
+        long long c_begin, c_end;
+        int grid;
+    };
+
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool use_graph = true;
+    std::vector<Req> reqs;  // in the order added
+    std::mutex mu;
+    std::string err;
+
+    // plan (rebuilt when requests change)
+    bool planned = false;
+    std::vector<Tree*> trees;
+    std::vector<int> order;          // sorted position -> request
+    std::vector<int> range_reqs;     // request indices of range requests, in order added
+    std::vector<Group> groups;
+    long long n_range_queries = 0, c2_end = 0;
+    int write_grid = 0;
+    char* dev = nullptr;             // one device allocation for the plan
+    DevTree* d_trees = nullptr;
+    BatchReq* d_reqs = nullptr;
+    long long* d_c1 = nullptr;
+    long long* d_c2 = nullptr;
+    int* d_ridx = nullptr;
+    long long* d_counts = nullptr;
+    long long* d_goff = nullptr;
+    long long* d_totals = nullptr;
+    unsigned long long* d_ctr = nullptr;
+    void* d_scan = nullptr;
+    DevStatus* d_st = nullptr;
+    DevTree* h_trees = nullptr;      // pinned: read by the graph's first copy
+    DevStatus* h_st = nullptr;       // pinned
+    std::vector<long long> h_totals;
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> ev_join;
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr, ev_t0 = nullptr;
+    std::vector<cudaEvent_t> ev_tree;
+    cudaGraphExec_t exec = nullptr;
+    bool launched = false;
+
+    void init(int dev_id) {
+        device = dev_id;
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+        CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+        CK(cudaMallocHost(&h_st, sizeof(DevStatus)));
+    }
+
+    void drop_plan() {
+        if (launched && ev_done != nullptr) cudaEventSynchronize(ev_done);
+        if (exec != nullptr) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        if (dev != nullptr) cudaFree(dev);
+        dev = nullptr;
+        if (h_trees != nullptr) cudaFreeHost(h_trees);
+        h_trees = nullptr;
+        for (auto s : branch) cudaStreamDestroy(s);
+        branch.clear();
+        for (auto e : ev_join) cudaEventDestroy(e);
+        ev_join.clear();
+        for (auto e : ev_tree) cudaEventDestroy(e);
+        ev_tree.clear();
+        planned = false;
+    }
+
+    void destroy() {
+        drop_plan();
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_done) cudaEventDestroy(ev_done);
+        if (h_st) cudaFreeHost(h_st);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+        ev_fork = ev_done = nullptr;
+        h_st = nullptr;
+        stream = nullptr;
+    }
+
+    int add(Req r) {
+        if (r.tree == nullptr) throw BadArg{"batch: null tree"};
+        if (r.tree->device != device) throw BadArg{"batch: tree lives on another device"};
+        drop_plan();
+        reqs.push_back(r);
+        return (int)reqs.size() - 1;
+    }
+
+    void clear() {
+        drop_plan();
+        reqs.clear();
+    }
+
+    int req_class(const Req& r) const { return r.d.kind == BATCH_KNN ? batch_kclass(r.d.k) : BATCH_RANGE_CLASS; }
+    int req_lanes(const Req& r) const {
+        if (r.d.kind != BATCH_KNN) return 1;
+        int l = r.lanes > 0 ? r.lanes : r.tree->knn_lanes;
+        return l >= 4 ? 4 : l >= 2 ? 2 : 1;
+    }
+
+    void plan() {
+        drop_plan();
+        const int n = (int)reqs.size();
+        trees.clear();
+        range_reqs.clear();
+        std::vector<int> tree_of(n);
+        for (int i = 0; i < n; ++i) {
+            auto it = std::find(trees.begin(), trees.end(), reqs[i].tree);
+            tree_of[i] = (int)(it - trees.begin());
+            if (it == trees.end()) trees.push_back(reqs[i].tree);
+            if (reqs[i].d.kind != BATCH_KNN) range_reqs.push_back(i);
+        }
+        order.resize(n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            int ka = req_class(reqs[a]) * 8 + req_lanes(reqs[a]), kb = req_class(reqs[b]) * 8 + req_lanes(reqs[b]);
+            return ka < kb;
+        });
+        // device descriptors, sorted order
+        std::vector<BatchReq> d(n);
+        std::vector<long long> c1(n);
+        groups.clear();
+        long long chunk = 0, cbase = 0;
+        for (int p = 0; p < n; ++p) {
+            Req& r = reqs[order[p]];
+            BatchReq b = r.d;
+            b.tree = tree_of[order[p]];
+            const int kc = req_class(r), lanes = req_lanes(r);
+            b.kclass = kc < BATCH_RANGE_CLASS ? kc : 0;
+            b.lanes = lanes;
+            const long long per = kc < BATCH_RANGE_CLASS ? BATCH_THREADS / lanes : BATCH_THREADS;
+            b.c1 = chunk;
+            b.n1 = (b.nq + per - 1) / per;
+            chunk += b.n1;
+            if (b.kind != BATCH_KNN) {
+                b.cbase = cbase;
+                cbase += b.nq;
+            }
+            if (groups.empty() || groups.back().kclass != kc || groups.back().lanes != lanes)
+                groups.push_back(Group{kc, lanes, p, p + 1, b.c1, chunk, 0});
+            else {
+                groups.back().r1 = p + 1;
+                groups.back().c_end = chunk;
+            }
+            d[p] = b;
+            c1[p] = b.c1;
+        }
+        n_range_queries = cbase;
+        // phase 2: range requests by c2
+        std::vector<int> ridx;
+        std::vector<long long> c2;
+        long long chunk2 = 0;
+        std::vector<int> pos_of(n);
+        for (int p = 0; p < n; ++p) pos_of[order[p]] = p;
+        for (size_t j = 0; j < range_reqs.size(); ++j) {
+            BatchReq& b = d[pos_of[range_reqs[j]]];
+            b.c2 = chunk2;
+            b.n2 = (b.nq + BATCH_THREADS - 1) / BATCH_THREADS;
+            if (b.n2 > 0) {
+                ridx.push_back(pos_of[range_reqs[j]]);
+                c2.push_back(chunk2);
+            }
+            chunk2 += b.n2;
+        }
+        c2_end = chunk2;
+        for (auto& g : groups) g.grid = batch_search_grid(g.kclass, g.lanes);
+        write_grid = batch_write_grid();
+        // one allocation for the plan
+        const size_t nt = trees.size(), nr = range_reqs.size();
+        size_t bytes = align_up(sizeof(DevTree) * nt) + align_up(sizeof(BatchReq) * n) +
+                       align_up(sizeof(long long) * n) + align_up(sizeof(long long) * (ridx.size() + 1)) +
+                       align_up(sizeof(int) * (ridx.size() + 1)) + 2 * align_up(sizeof(long long) * (cbase + 1)) +
+                       align_up(sizeof(long long) * (nr + 1)) + align_up(sizeof(unsigned long long) * 64) +
+                       align_up(scan_temp_bytes(cbase + 1)) + align_up(sizeof(DevStatus)) + 4096;
+        CK(cudaMalloc(&dev, bytes));
+        Carver c(dev);
+        d_trees = c.take<DevTree>(nt);
+        d_reqs = c.take<BatchReq>(n);
+        d_c1 = c.take<long long>(n);
+        d_c2 = c.take<long long>(ridx.size() + 1);
+        d_ridx = c.take<int>(ridx.size() + 1);
+        d_counts = c.take<long long>(cbase + 1);
+        d_goff = c.take<long long>(cbase + 1);
+        d_totals = c.take<long long>(nr + 1);
+        d_ctr = c.take<unsigned long long>(64);
+        d_scan = c.take<char>(scan_temp_bytes(cbase + 1));
+        d_st = c.take<DevStatus>(1);
+        for (size_t j = 0; j < nr; ++j) d[pos_of[range_reqs[j]]].total = d_totals + j;
+        CK(cudaMallocHost(&h_trees, sizeof(DevTree) * std::max<size_t>(nt, 1)));
+        CK(cudaMemcpyAsync(d_reqs, d.data(), sizeof(BatchReq) * n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d_c1, c1.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, stream));
+        if (!ridx.empty()) {
+            CK(cudaMemcpyAsync(d_c2, c2.data(), sizeof(long long) * c2.size(), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(d_ridx, ridx.data(), sizeof(int) * ridx.size(), cudaMemcpyHostToDevice, stream));
+        }
+        CK(cudaMemsetAsync(d_counts, 0, sizeof(long long) * (cbase + 1), stream));
+        CK(cudaMemsetAsync(d_totals, 0, sizeof(long long) * (nr + 1), stream));
+        CK(cudaStreamSynchronize(stream));  // d and the vectors above live on this frame
+        h_totals.assign(nr, 0);
+        nridx = (int)ridx.size();
+        for (size_t g = 1; g < groups.size(); ++g) {
+            cudaStream_t bs;
+            CK(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+            branch.push_back(bs);
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ev_join.push_back(e);
+        }
+        for (size_t i = 0; i < nt; ++i) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ev_tree.push_back(e);
+        }
+        planned = true;
+        if (use_graph) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue();
+            } catch (...) {
+                cudaStreamEndCapture(stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            CK(cudaStreamEndCapture(stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            CK(e);
+        }
+    }
+    int nridx = 0;
+
+    // The work of one run, on `stream` (captured into the graph, or issued
+    // directly when graphs are off).
+    void enqueue() {
+        CK(cudaMemcpyAsync(d_trees, h_trees, sizeof(DevTree) * trees.size(), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(d_ctr, 0, sizeof(unsigned long long) * 64, stream));
+        CK(cudaMemsetAsync(d_st, 0, sizeof(DevStatus), stream));
+        if (groups.size() > 1) CK(cudaEventRecord(ev_fork, stream));
+        for (size_t g = 0; g < groups.size(); ++g) {
+            const Group& G = groups[g];
+            cudaStream_t s = g == 0 ? stream : branch[g - 1];
+            if (g > 0) CK(cudaStreamWaitEvent(s, ev_fork, 0));
+            launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes, d_counts,
+                                d_ctr + g, G.grid, s);
+            if (g > 0) CK(cudaEventRecord(ev_join[g - 1], s));
+        }
+        for (size_t g = 1; g < groups.size(); ++g) CK(cudaStreamWaitEvent(stream, ev_join[g - 1], 0));
+        if (nridx > 0) {
+            exclusive_scan(d_counts, d_goff, n_range_queries + 1, nullptr, d_scan, stream);
+            launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid, stream);
+        }
+        // range requests without queries: empty CSR
+        for (int j : range_reqs)
+            if (reqs[j].d.nq == 0) CK(cudaMemsetAsync(reqs[j].d.offsets, 0, sizeof(long long), stream));
+        CK(cudaGetLastError());
+    }
+
+    void run() {
+        if (reqs.empty()) return;
+        if (!planned) plan();
+        // the previous run's copy of h_trees must be done before it changes
+        if (launched) CK(cudaEventSynchronize(ev_done));
+        for (size_t i = 0; i < trees.size(); ++i) {
+            Tree* t = trees[i];
+            std::lock_guard<std::mutex> lock(t->mu);
+            h_trees[i] = t->dt;
+            h_trees[i].st = d_st;
+            CK(cudaEventRecord(ev_tree[i], t->stream));
+            CK(cudaStreamWaitEvent(stream, ev_tree[i], 0));
+        }
+        if (use_graph)
+            CK(cudaGraphLaunch(exec, stream));
+        else
+            enqueue();
+        CK(cudaEventRecord(ev_done, stream));
+        launched = true;
+        // later work on each tree (mutations) waits for this run
+        for (Tree* t : trees) {
+            std::lock_guard<std::mutex> lock(t->mu);
+            CK(cudaStreamWaitEvent(t->stream, ev_done, 0));
+        }
+    }
+
+    // Waits for the last run; fills totals (one per range request, in the
+    // order added).  Returns false when a range request overflowed.
+    bool synchronize(long long* totals) {
+        CK(cudaStreamSynchronize(stream));
+        if (!planned) return true;
+        CK(cudaMemcpy(h_st, d_st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+        if (!range_reqs.empty())
+            CK(cudaMemcpy(h_totals.data(), d_totals, sizeof(long long) * range_reqs.size(), cudaMemcpyDeviceToHost));
+        if (totals)
+            for (size_t j = 0; j < h_totals.size(); ++j) totals[j] = h_totals[j];
+        if (h_st->err & (ERR_STACK | ERR_LOOP)) throw Internal{"batch: traversal stack overflow or loop cap"};
+        return !(h_st->err & ERR_OUTPUT);
+    }
+
+    // Median time (ms) of `reps` runs of this batch, on its stream.
+    float time_runs(int reps) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        std::vector<float> ts;
+        run();
+        synchronize(nullptr);
+        for (int i = 0; i < reps; ++i) {
+            CK(cudaEventRecord(a, stream));
+            run();
+            CK(cudaEventRecord(b, stream));
+            CK(cudaEventSynchronize(b));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            ts.push_back(ms);
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        synchronize(nullptr);
+        std::sort(ts.begin(), ts.end());
+        return ts[ts.size() / 2];
+    }
+};
+
+// Per tree of the batch: the leaf fill (points per leaf when the tree is
+// rebuilt, 8..32) and the lanes per kNN query (1, 2, 4) with the fastest
+// median run of that tree's requests alone.  Leaves the tree rebuilt at the
+// chosen fill and the requests at the chosen lanes.
+void autotune_batch(Batch& b, int reps, const std::vector<int>& fills, const std::vector<int>& lanes_set,
+                    int* chosen) {
+    std::vector<Tree*> ts;
+    for (auto& r : b.reqs)
+        if (std::find(ts.begin(), ts.end(), r.tree) == ts.end()) ts.push_back(r.tree);
+    for (size_t ti = 0; ti < ts.size(); ++ti) {
+        Tree* t = ts[ti];
+        Batch sub;
+        sub.init(b.device);
+        std::vector<int> map;
+        for (size_t i = 0; i < b.reqs.size(); ++i)
+            if (b.reqs[i].tree == t) {
+                sub.reqs.push_back(b.reqs[i]);
+                map.push_back((int)i);
+            }
+        bool has_knn = false;
+        for (auto& r : sub.reqs) has_knn |= r.d.kind == BATCH_KNN;
+        float best = 1e30f;
+        int best_fill = t->fill, best_lanes = 1;
+        try {
+            for (int f : fills) {
+                {
+                    std::lock_guard<std::mutex> lock(t->mu);
+                    t->fill = f;
+                    t->rebuild_all();
+                }
+                for (int l : lanes_set) {
+                    if (!has_knn && l != lanes_set.front()) continue;
+                    for (auto& r : sub.reqs) r.lanes = l;
+                    sub.drop_plan();
+                    float ms = sub.time_runs(reps);
+                    if (ms < best) {
+                        best = ms;
+                        best_fill = f;
+                        best_lanes = l;
+                    }
+                }
+            }
+            {
+                std::lock_guard<std::mutex> lock(t->mu);
+                t->fill = best_fill;
+                t->rebuild_all();
+            }
+        } catch (...) {
+            sub.destroy();
+            throw;
+        }
+        sub.destroy();
+        for (int i : map)
+            if (b.reqs[i].d.kind == BATCH_KNN) b.reqs[i].lanes = best_lanes;
+        if (chosen != nullptr) {
+            chosen[2 * ti] = best_fill;
+            chosen[2 * ti + 1] = best_lanes;
+        }
+    }
+    b.drop_plan();
+}
+
 }  // namespace ikdg
 
 struct ikdg_tree {
     ikdg::Tree t;
+};
+
+struct ikdg_batch {
+    ikdg::Batch b;
 };
 
 namespace {
@@ -919,6 +1375,31 @@ int guarded(ikdg_tree* h, F&& f) {
         return fail(h, IKDG_INTERNAL, e.what);
     } catch (const std::bad_alloc&) {
         return fail(h, IKDG_INTERNAL, "host allocation failed");
+    }
+}
+
+template <class F>
+int batch_guarded(ikdg_batch* h, F&& f) {
+    if (h == nullptr) return IKDG_BAD_ARG;
+    std::lock_guard<std::mutex> lock(h->b.mu);
+    auto bfail = [&](int code, const std::string& msg) {
+        h->b.err = msg;
+        return code;
+    };
+    try {
+        CK(cudaSetDevice(h->b.device));
+        f(h->b);
+        return IKDG_OK;
+    } catch (const ikdg::CudaFail& e) {
+        return bfail(IKDG_CUDA_ERR, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+    } catch (const ikdg::BadArg& e) {
+        return bfail(IKDG_BAD_ARG, e.what);
+    } catch (const ikdg::CapacityFail& e) {
+        return bfail(IKDG_CAPACITY, e.what);
+    } catch (const ikdg::Internal& e) {
+        return bfail(IKDG_INTERNAL, e.what);
+    } catch (const std::bad_alloc&) {
+        return bfail(IKDG_INTERNAL, "host allocation failed");
     }
 }
 
@@ -1197,6 +1678,185 @@ int ikdg_synchronize(ikdg_tree* h) {
     return guarded(h, [&](ikdg::Tree& t) {
         CK(cudaStreamSynchronize(t.stream));
         CK(cudaGetLastError());
+    });
+}
+
+int ikdg_box_search_device(ikdg_tree* h, const float* boxes, int64_t nb, int64_t* offsets, int32_t* ids, float* xyz,
+                           int64_t capacity, int64_t* total) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        t.range_device(0, boxes, nb, 6, nullptr, 0, (long long*)offsets, ids, xyz, capacity, (long long*)total);
+    });
+}
+
+int ikdg_radius_search_device(ikdg_tree* h, const float* centers, int64_t nq, int32_t stride, const float* radius,
+                              int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
+                              int64_t* total) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        t.range_device(1, centers, nq, stride, radius, radius_stride, (long long*)offsets, ids, xyz, capacity,
+                       (long long*)total);
+    });
+}
+
+// ---- multi-tree batches ------------------------------------------------------------
+
+const char* ikdg_batch_last_error(const ikdg_batch* b) { return b ? b->b.err.c_str() : "null batch"; }
+
+int ikdg_batch_create(int device, ikdg_batch** out) {
+    if (out == nullptr) return IKDG_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return IKDG_NO_DEVICE;
+    }
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return IKDG_NO_DEVICE;
+    if (device >= ndev) return IKDG_BAD_ARG;
+    ikdg_batch* h = new (std::nothrow) ikdg_batch;
+    if (h == nullptr) return IKDG_INTERNAL;
+    try {
+        h->b.init(device);
+    } catch (...) {
+        h->b.destroy();
+        delete h;
+        return IKDG_CUDA_ERR;
+    }
+    *out = h;
+    return IKDG_OK;
+}
+
+int ikdg_batch_destroy(ikdg_batch* h) {
+    if (h == nullptr) return IKDG_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lock(h->b.mu);
+        cudaSetDevice(h->b.device);
+        h->b.destroy();
+    }
+    delete h;
+    return IKDG_OK;
+}
+
+int ikdg_batch_clear(ikdg_batch* h) {
+    return batch_guarded(h, [&](ikdg::Batch& b) { b.clear(); });
+}
+
+int ikdg_batch_add_knn(ikdg_batch* h, ikdg_tree* tree, const float* queries, int64_t nq, int32_t stride, int32_t k,
+                       double max_dist, int32_t* ids, float* d2, float* xyz, int32_t* counts, int32_t* request) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (tree == nullptr || nq < 0 || stride < 3 || k < 1 ||
+            (nq > 0 && (queries == nullptr || ids == nullptr || d2 == nullptr)))
+            throw ikdg::BadArg{"batch_add_knn: bad arguments"};
+        if (k > ikdg::BATCH_KMAX) throw ikdg::BadArg{"batch_add_knn: k must be <= 16"};
+        ikdg::Batch::Req r;
+        r.tree = &tree->t;
+        r.max_dist = max_dist;
+        r.d.kind = ikdg::BATCH_KNN;
+        r.d.q = queries;
+        r.d.nq = nq;
+        r.d.q_stride = stride;
+        r.d.k = k;
+        r.d.max_sq = ikdg::max_sq_threshold(max_dist);
+        r.d.ids = ids;
+        r.d.d2 = d2;
+        r.d.xyz = xyz;
+        r.d.cnt = counts;
+        int id = b.add(r);
+        if (request) *request = id;
+    });
+}
+
+int ikdg_batch_add_box_search(ikdg_batch* h, ikdg_tree* tree, const float* boxes, int64_t nb, int64_t* offsets,
+                              int32_t* ids, float* xyz, int64_t capacity, int32_t* request) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (tree == nullptr || nb < 0 || offsets == nullptr || capacity < 0 || (nb > 0 && boxes == nullptr) ||
+            (capacity > 0 && ids == nullptr))
+            throw ikdg::BadArg{"batch_add_box_search: bad arguments"};
+        ikdg::Batch::Req r;
+        r.tree = &tree->t;
+        r.d.kind = ikdg::BATCH_BOX;
+        r.d.q = boxes;
+        r.d.nq = nb;
+        r.d.q_stride = 6;
+        r.d.ids = ids;
+        r.d.xyz = xyz;
+        r.d.offsets = (long long*)offsets;
+        r.d.capacity = capacity;
+        int id = b.add(r);
+        if (request) *request = id;
+    });
+}
+
+int ikdg_batch_add_radius_search(ikdg_batch* h, ikdg_tree* tree, const float* centers, int64_t nq, int32_t stride,
+                                 const float* radius, int32_t radius_stride, int64_t* offsets, int32_t* ids,
+                                 float* xyz, int64_t capacity, int32_t* request) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (tree == nullptr || nq < 0 || stride < 3 || radius_stride < 0 || offsets == nullptr || capacity < 0 ||
+            (nq > 0 && (centers == nullptr || radius == nullptr)) || (capacity > 0 && ids == nullptr))
+            throw ikdg::BadArg{"batch_add_radius_search: bad arguments"};
+        ikdg::Batch::Req r;
+        r.tree = &tree->t;
+        r.d.kind = ikdg::BATCH_RADIUS;
+        r.d.q = centers;
+        r.d.nq = nq;
+        r.d.q_stride = stride;
+        r.d.radius = radius;
+        r.d.r_stride = radius_stride;
+        r.d.ids = ids;
+        r.d.xyz = xyz;
+        r.d.offsets = (long long*)offsets;
+        r.d.capacity = capacity;
+        int id = b.add(r);
+        if (request) *request = id;
+    });
+}
+
+int ikdg_batch_set_knn_lanes(ikdg_batch* h, int32_t request, int32_t lanes) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (request < 0 || request >= (int)b.reqs.size() || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4))
+            throw ikdg::BadArg{"batch_set_knn_lanes: bad arguments"};
+        b.reqs[request].lanes = lanes;
+        b.drop_plan();
+    });
+}
+
+int ikdg_batch_set_graph(ikdg_batch* h, int use_graph) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        b.drop_plan();
+        b.use_graph = use_graph != 0;
+    });
+}
+
+int ikdg_batch_run(ikdg_batch* h) {
+    return batch_guarded(h, [&](ikdg::Batch& b) { b.run(); });
+}
+
+int ikdg_batch_synchronize(ikdg_batch* h, int64_t* range_totals) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (!b.synchronize((long long*)range_totals))
+            throw ikdg::CapacityFail{"batch: a range request's results exceed its capacity"};
+    });
+}
+
+int ikdg_batch_autotune(ikdg_batch* h, int32_t reps, int32_t* chosen) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (reps < 1) throw ikdg::BadArg{"batch_autotune: reps must be >= 1"};
+        ikdg::autotune_batch(b, reps, {8, 12, 16, 24, 32}, {1, 2, 4}, chosen);
+    });
+}
+
+int ikdg_batch_num_trees(ikdg_batch* h, int32_t* n) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (n == nullptr) throw ikdg::BadArg{"batch_num_trees: null output"};
+        std::vector<ikdg::Tree*> ts;
+        for (auto& r : b.reqs)
+            if (std::find(ts.begin(), ts.end(), r.tree) == ts.end()) ts.push_back(r.tree);
+        *n = (int32_t)ts.size();
+    });
+}
+
+int ikdg_batch_get_stream(ikdg_batch* h, void** stream) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (stream == nullptr) throw ikdg::BadArg{"batch_get_stream: null output"};
+        *stream = (void*)b.stream;
     });
 }
 

@@ -8,10 +8,11 @@
 namespace ikdg {
 
 // ---- scan.cu / sort.cu ------------------------------------------------------
-// Exclusive prefix sum of n int32 values; `total` (device, nullable) receives
+// Exclusive prefix sum of n int32 / int64 values; `total` (device, nullable) receives
 // the sum.  `temp` must hold scan_temp_bytes(n) bytes.
 size_t scan_temp_bytes(long long n);
 void exclusive_scan(const int* in, int* out, long long n, int* total, void* temp, cudaStream_t s);
+void exclusive_scan(const long long* in, long long* out, long long n, long long* total, void* temp, cudaStream_t s);
 
 // Stable LSD radix sort of `batch` independent (key, value) arrays of length n
 // stored `stride` elements apart, on the low `bits` bits of the key (a
@@ -69,10 +70,58 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
 // Box (mode 0) and radius (mode 1) search.  Pass 1 (ids == nullptr) writes
 // per-query hit counts into `counts`; pass 2 writes ids / xyz starting at
 // offsets[i].  Boxes are {min xyz, max xyz}; radius queries are {x, y, z} with
-// a per-query radius.
-void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius,
+// a per-query radius (r_stride floats apart).  With capacity >= 0, pass 2
+// reads counts and skips (raising ERR_OUTPUT) every query whose results would
+// end past `capacity`.
+void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius, int r_stride,
                   long long nq, long long* counts, const long long* offsets, int* ids, float* xyz,
-                  cudaStream_t s);
+                  long long capacity, cudaStream_t s);
+
+// ---- batch.cu ---------------------------------------------------------------------
+// One request of a multi-tree batch: a kNN, box or radius search of nq queries
+// on trees[tree].  Phase 1 (search) covers chunks [c1, c1 + n1) of the
+// phase's chunk numbering; range requests also take phase-2 (write) chunks
+// [c2, c2 + n2).  A chunk is BATCH_THREADS threads: 128 / lanes kNN queries,
+// or 128 range queries.
+constexpr int BATCH_THREADS = 128;
+constexpr int BATCH_KMAX = 16;
+constexpr int BATCH_RANGE_CLASS = 5;  // register class of box / radius requests
+enum BatchKind : int { BATCH_KNN = 0, BATCH_BOX = 1, BATCH_RADIUS = 2 };
+
+struct BatchReq {
+    long long c1, n1, c2, n2;
+    const float* q;
+    const float* radius;
+    long long nq;
+    int kind, tree, q_stride, r_stride;
+    int k, kclass, lanes;
+    float max_sq;
+    int* ids;
+    float* d2;
+    float* xyz;
+    int* cnt;
+    long long* offsets;  // range: nq + 1 entries, CSR within the request
+    long long cbase;     // range: first entry of this request in the batch count array
+    long long capacity;  // range: ids / xyz capacity
+    long long* total;    // range: device total (nullable)
+};
+
+// Register class of a kNN request with this k (k <= BATCH_KMAX): 0..4;
+// range requests are class BATCH_RANGE_CLASS.
+int batch_kclass(int k);
+// Resident CTAs (whole GPU) of the persistent search kernel of a class.
+int batch_search_grid(int kclass, int lanes);
+int batch_write_grid();
+// Phase 1 over requests [r0, r1), all of register class kclass and `lanes`
+// lanes per query, whose chunks are [c_begin, c_end); ctr: a zeroed device
+// counter.
+void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
+                         long long c_begin, long long c_end, int kclass, int lanes, long long* counts,
+                         unsigned long long* ctr, int grid, cudaStream_t s);
+// Phase 2 over the range requests listed in ridx[0..nr) (ascending c2, chunks
+// [0, c_end)); goff: exclusive scan of the batch count array.
+void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
+                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s);
 
 // ---- register.cu ---------------------------------------------------------------
 // Rt_dev: 12 doubles, R row-major then t.  planes: 2 float4 per point ({n,d}

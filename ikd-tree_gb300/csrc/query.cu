@@ -1,45 +1,16 @@
-// Batched searches: Nearest_Search, Box_Search, Radius_Search.
-//
-// Semantics (the drop-in contract):
-//   * kNN (Nearest_Search / Search, ikd-Tree/ikd_Tree.cpp:366-397, :868-1013):
-//     the k valid points with the smallest squared distance, among those with
-//     sq_dist <= max_dist^2, ascending.  Ties at equal distance are broken by
-//     the smaller point id (the reference leaves them to traversal order).  A
-//     subtree is skipped only when its AABB lower bound exceeds the current
-//     k-th distance or max_dist^2, so the result is exact.
-//   * Box_Search (:399-404, :1015-1044): every valid p with min <= p < max.
-//   * Radius_Search (:406-411, :1046-1087): every valid p with
-//     sq_dist(p, q) <= r*r in float.  Whole subtrees are taken when their
-//     farthest corner is inside (an exact float bound), so no point at the
-//     boundary is admitted or lost by rounding.
+// Batched searches: Nearest_Search, Box_Search, Radius_Search, one launch per
+// call; the traversal bodies and their semantics are in search.cuh.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
-#include "kernels.cuh"
+#include "search.cuh"
 
 namespace ikdg {
 namespace {
 
-constexpr float FINF = __builtin_huge_valf();
+using search::FINF;
 
-__device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
-    return d < d2 || (d == d2 && id < id2);
-}
-
-// KMAX > 0: the best k candidates live sorted in registers (k <= KMAX).
-// KMAX == 0: any k; the sorted candidates live in the query's output rows
-// (global memory), with the slot index parked in out_cnt-independent scratch
-// `slots` (k ints per query).
-// Traversal of one query by a group of G consecutive lanes: nearer child
-// first, the farther one pushed with its box distance; a subtree is skipped
-// when that distance exceeds min(max_dist^2, current k-th distance).  The loop
-// is "while-while": a node phase steps every group through nodes until it holds
-// a leaf (or is finished), then the warp scans leaves together, so the leaf
-// scans run with most lanes active.  The G lanes of a group keep identical
-// copies of the traversal state; in a leaf, lane s takes slots s, s+G, ...
-// and the G candidates of each round are broadcast and offered to every copy
-// in lane order, which keeps the copies identical.
 template <int KMAX, int G>
 __global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
                                                   long long nq, int k, float max_sq, int* __restrict__ out_id,
@@ -47,320 +18,39 @@ __global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __rest
                                                   int* __restrict__ out_cnt, int* __restrict__ slots,
                                                   const int* __restrict__ perm) {
     const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long tid = gtid / G;
-    const int sub = threadIdx.x & (G - 1);
-    const int lane = threadIdx.x & 31;
-    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-    const bool valid = tid < nq;
-    long long qi = valid ? tid : 0;
-    if (valid && perm != nullptr) qi = __ldg(perm + tid);
-    const float qx = valid ? q[qi * q_stride + 0] : 0.f;
-    const float qy = valid ? q[qi * q_stride + 1] : 0.f;
-    const float qz = valid ? q[qi * q_stride + 2] : 0.f;
-
-    constexpr int KR = KMAX > 0 ? KMAX : 1;
-    float bd[KR];
-    int bi[KR], bsl[KR];
-#pragma unroll
-    for (int j = 0; j < KR; ++j) {
-        bd[j] = FINF;
-        bi[j] = 0x7fffffff;
-        bsl[j] = -1;
-    }
-    float* gd = out_d2 + qi * k;
-    int* gi = out_id + qi * k;
-    int* gs = slots != nullptr ? slots + qi * k : nullptr;
-    int gcnt = 0;
-    float worst = FINF;
-    int worst_id = 0x7fffffff;
-
-    int st_code[MAX_STACK];
-    float st_d[MAX_STACK];
-    int sp = 0;
-    int cur = 0;  // node code (>= 0; 0 = the sentinel record) or leaf code (< 0)
-    bool done = !valid;
-    int visits = 0;
-    const float4* __restrict__ P = t.pts;
-
-    // Next stacked subtree that can still hold a result, or done.
-    auto pop = [&]() {
-        const float lim = fminf(max_sq, worst);
-        while (sp > 0) {
-            --sp;
-            if (st_d[sp] <= lim) {
-                cur = st_code[sp];
-                return;
-            }
-        }
-        done = true;
-    };
-
-    // Offers a candidate to this lane's copy of the k best.
-    auto offer = [&](float d, int id, int sl) {
-        if (!(d <= max_sq && cand_less(d, id, worst, worst_id))) return;
-        if (KMAX == 0) {
-            // Large k: the sorted list lives in the output rows; only the
-            // group's first lane owns them.
-            if (sub == 0) {
-                int pos = gcnt < k ? gcnt : k - 1;
-                while (pos > 0 && cand_less(d, id, gd[pos - 1], gi[pos - 1])) {
-                    gd[pos] = gd[pos - 1];
-                    gi[pos] = gi[pos - 1];
-                    gs[pos] = gs[pos - 1];
-                    --pos;
-                }
-                gd[pos] = d;
-                gi[pos] = id;
-                gs[pos] = sl;
-            }
-            if (gcnt < k) ++gcnt;
-            if (gcnt == k) {
-                __syncwarp(gmask);
-                worst = __shfl_sync(gmask, sub == 0 ? gd[k - 1] : 0.f, lane & ~(G - 1));
-                worst_id = __shfl_sync(gmask, sub == 0 ? gi[k - 1] : 0, lane & ~(G - 1));
-            }
-            return;
-        }
-        float cd = d;
-        int cid = id, cs = sl;
-#pragma unroll
-        for (int m = 0; m < KR; ++m) {
-            const bool sw = cand_less(cd, cid, bd[m], bi[m]);
-            const float td = bd[m];
-            const int ti = bi[m], ts = bsl[m];
-            bd[m] = sw ? cd : td;
-            bi[m] = sw ? cid : ti;
-            bsl[m] = sw ? cs : ts;
-            cd = sw ? td : cd;
-            cid = sw ? ti : cid;
-            cs = sw ? ts : cs;
-        }
-#pragma unroll
-        for (int m = 0; m < KR; ++m)
-            if (m == k - 1) {
-                worst = bd[m];
-                worst_id = bi[m];
-            }
-    };
-
-    while (true) {
-        // Node phase.
-        while (true) {
-            const bool nodework = !done && cur >= 0;
-            if (!__any_sync(0xffffffffu, nodework)) break;
-            if (!nodework) continue;
-            if (++visits > MAX_VISITS) {
-                atomicOr(&t.st->err, ERR_LOOP);
-                done = true;
-                continue;
-            }
-            NodeRec r = load_node(t.node, cur);
-            const int cl = r.left(), cr = r.right();
-            const float lim = fminf(max_sq, worst);
-            float dl = FINF, dr = FINF;
-            bool vl = false, vr = false;
-            if (cl != 0 && r.f0.x <= r.f0.w) {
-                dl = box_dist(qx, qy, qz, r.f0.x, r.f0.y, r.f0.z, r.f0.w, r.f1.x, r.f1.y);
-                vl = dl <= lim;
-            }
-            if (cr != 0 && r.f1.z <= r.f2.y) {
-                dr = box_dist(qx, qy, qz, r.f1.z, r.f1.w, r.f2.x, r.f2.y, r.f2.z, r.f2.w);
-                vr = dr <= lim;
-            }
-            if (vl && vr) {
-                const bool left_first = dl <= dr;
-                if (sp < MAX_STACK) {
-                    st_code[sp] = left_first ? cr : cl;
-                    st_d[sp] = left_first ? dr : dl;
-                    ++sp;
-                } else {
-                    atomicOr(&t.st->err, ERR_STACK);
-                }
-                cur = left_first ? cl : cr;
-            } else if (vl) {
-                cur = cl;
-            } else if (vr) {
-                cur = cr;
-            } else {
-                pop();
-            }
-        }
-        // Leaf phase.
-        const bool leafwork = !done && cur < 0;
-        if (!__any_sync(0xffffffffu, leafwork)) break;
-        if (!leafwork) continue;
-        const int L = code_leaf(cur);
-        const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
-        const float4* lp = P + (long long)L * LEAF_CAP;
-        for (int j0 = 0; j0 < n; j0 += G) {
-            const int j = j0 + sub;
-            float d = FINF;
-            int id = 0x7fffffff, sl = -1;
-            if (j < n) {
-                const float4 p = __ldg(lp + j);
-                const uint32_t w = __float_as_uint(p.w);
-                if (!(w & F_DEL)) {
-                    d = sq_dist(qx, qy, qz, p.x, p.y, p.z);
-                    id = (int)(w & ID_MASK);
-                    sl = L * LEAF_CAP + j;
-                }
-            }
-            if (G == 1) {
-                if (sl >= 0) offer(d, id, sl);
-            } else {
-#pragma unroll
-                for (int s = 0; s < G; ++s) {
-                    const int src = (lane & ~(G - 1)) + s;
-                    const float ds = __shfl_sync(gmask, d, src);
-                    const int is = __shfl_sync(gmask, id, src);
-                    const int ss = __shfl_sync(gmask, sl, src);
-                    if (ss >= 0) offer(ds, is, ss);
-                }
-            }
-        }
-        pop();
-    }
-    if (!valid || sub != 0) return;
-
-    if (KMAX == 0) {
-        for (int j = 0; j < k; ++j) {
-            const bool ok = j < gcnt;
-            const int sl = ok ? gs[j] : -1;
-            if (!ok) {
-                gi[j] = -1;
-                gd[j] = FINF;
-            }
-            if (out_xyz != nullptr) {
-                float4 p = ok ? __ldg(P + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
-                out_xyz[(qi * k + j) * 3 + 0] = p.x;
-                out_xyz[(qi * k + j) * 3 + 1] = p.y;
-                out_xyz[(qi * k + j) * 3 + 2] = p.z;
-            }
-        }
-        if (out_cnt != nullptr) out_cnt[qi] = gcnt;
-        return;
-    }
-    int cnt = 0;
-#pragma unroll
-    for (int j = 0; j < KR; ++j) {
-        if (j < k) {
-            const bool ok = bsl[j] >= 0;
-            out_id[qi * k + j] = ok ? bi[j] : -1;
-            out_d2[qi * k + j] = ok ? bd[j] : FINF;
-            if (out_xyz != nullptr) {
-                float4 p = ok ? __ldg(P + bsl[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
-                out_xyz[(qi * k + j) * 3 + 0] = p.x;
-                out_xyz[(qi * k + j) * 3 + 1] = p.y;
-                out_xyz[(qi * k + j) * 3 + 2] = p.z;
-            }
-            cnt += ok ? 1 : 0;
-        }
-    }
-    if (out_cnt != nullptr) out_cnt[qi] = cnt;
+    search::knn_body<KMAX, G>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots,
+                              perm);
 }
 
-// MODE 0: box, MODE 1: radius.  WRITE = false counts, true emits.
+// WRITE = false stores counts[qi]; true emits at [offsets[qi],
+// offsets[qi + 1]) (offsets has nq + 1 entries).  With a capacity (>= 0), a
+// query whose results would end past it writes nothing and raises ERR_OUTPUT.
 template <int MODE, bool WRITE>
 __global__ void __launch_bounds__(128) range_kernel(DevTree t, const float* __restrict__ q, int q_stride,
-                                                    const float* __restrict__ radius, long long nq,
+                                                    const float* __restrict__ radius, int r_stride, long long nq,
                                                     long long* __restrict__ counts,
                                                     const long long* __restrict__ offsets, int* __restrict__ ids,
-                                                    float* __restrict__ xyz) {
-    long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= nq) return;
-    Box3 qb;
-    float cx = 0.f, cy = 0.f, cz = 0.f, r2 = 0.f;
-    if (MODE == 0) {
-        for (int a = 0; a < 3; ++a) {
-            qb.lo[a] = q[qi * q_stride + a];
-            qb.hi[a] = q[qi * q_stride + 3 + a];
-        }
-    } else {
-        cx = q[qi * q_stride + 0];
-        cy = q[qi * q_stride + 1];
-        cz = q[qi * q_stride + 2];
-        const float r = radius[qi];
-        r2 = __fmul_rn(r, r);
+                                                    float* __restrict__ xyz, long long capacity) {
+    // No early exit: the search body is warp-collective.
+    const long long qi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = qi < nq;
+    if (!WRITE) {
+        const long long c =
+            search::range_body<MODE, false>(t, q, q_stride, radius, r_stride, qi, valid, 0, 0, nullptr, nullptr);
+        if (valid) counts[qi] = c;
+        return;
     }
-    long long count = 0;
-    long long o = WRITE ? offsets[qi] : 0;
-    int stack[MAX_STACK];
-    int sp = 0;
-    int cur = 0;        // code; the sentinel record first
-    bool covered = false;
-    bool is_start = true;
-    const float4* __restrict__ P = t.pts;
-    int visits = 0;
-    while (true) {
-        if (++visits > MAX_VISITS) {
-            atomicOr(&t.st->err, ERR_LOOP);
-            break;
+    long long o = 0, o_lim = 0;
+    bool go = valid;
+    if (valid) {
+        o = offsets[qi];
+        o_lim = offsets[qi + 1];
+        if (capacity >= 0 && o_lim > capacity) {
+            atomicOr(&t.st->err, ERR_OUTPUT);
+            go = false;
         }
-        if (is_start || cur > 0) {
-            const int X = is_start ? 0 : cur;
-            is_start = false;
-            NodeRec r = load_node(t.node, X);
-            int4 c4 = WRITE ? make_int4(0, 0, 0, 0) : __ldg(t.ncnt + X);
-#pragma unroll
-            for (int side = 0; side < 2; ++side) {
-                const int c = side == 0 ? r.left() : r.right();
-                if (c == 0) continue;
-                const Box3 b = r.box(side);
-                if (box_empty(b)) continue;
-                bool cov = covered;
-                if (!cov) {
-                    if (MODE == 0) {
-                        if (qbox_disjoint(qb, b)) continue;
-                        cov = qbox_covers(qb, b);
-                    } else {
-                        if (box_dist(cx, cy, cz, b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]) > r2) continue;
-                        cov = box_far(cx, cy, cz, b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]) <= r2;
-                    }
-                }
-                if (cov && !WRITE) {
-                    count += side == 0 ? (c4.x - c4.y) : (c4.z - c4.w);
-                    continue;
-                }
-                if (sp < MAX_STACK) {
-                    stack[sp++] = c * 2 + (cov ? 1 : 0);
-                } else {
-                    atomicOr(&t.st->err, ERR_STACK);
-                }
-            }
-        } else {
-            const int L = code_leaf(cur);
-            const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
-            const float4* lp = P + (long long)L * LEAF_CAP;
-            for (int j = 0; j < n; ++j) {
-                const float4 p = __ldg(lp + j);
-                const uint32_t w = __float_as_uint(p.w);
-                if (w & F_DEL) continue;
-                bool in = covered;
-                if (!in) {
-                    if (MODE == 0)
-                        in = qbox_holds(qb, p.x, p.y, p.z);
-                    else
-                        in = sq_dist(p.x, p.y, p.z, cx, cy, cz) <= r2;
-                }
-                if (!in) continue;
-                if (WRITE) {
-                    ids[o] = (int)(w & ID_MASK);
-                    if (xyz != nullptr) {
-                        xyz[o * 3 + 0] = p.x;
-                        xyz[o * 3 + 1] = p.y;
-                        xyz[o * 3 + 2] = p.z;
-                    }
-                    ++o;
-                }
-                ++count;
-            }
-        }
-        if (sp == 0) break;
-        const int item = stack[--sp];
-        cur = item >> 1;
-        covered = item & 1;
     }
-    if (!WRITE) counts[qi] = count;
+    search::range_body<MODE, true>(t, q, q_stride, radius, r_stride, qi, go, o, o_lim, ids, xyz);
 }
 
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -498,21 +188,25 @@ cudaError_t noalloc_scratch(int device, void** ptr) {
 
 size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_BYTES; }
 
-void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius, long long nq,
-                  long long* counts, const long long* offsets, int* ids, float* xyz, cudaStream_t s) {
+void launch_range(const DevTree& t, int mode, const float* q, int q_stride, const float* radius, int r_stride,
+                  long long nq, long long* counts, const long long* offsets, int* ids, float* xyz,
+                  long long capacity, cudaStream_t s) {
     if (nq <= 0) return;
     unsigned g = blocks_for(nq, 128);
+#define IKDG_RANGE(M, W) \
+    range_kernel<M, W><<<g, 128, 0, s>>>(t, q, q_stride, radius, r_stride, nq, counts, offsets, ids, xyz, capacity)
     if (mode == 0) {
         if (ids == nullptr)
-            range_kernel<0, false><<<g, 128, 0, s>>>(t, q, q_stride, radius, nq, counts, offsets, ids, xyz);
+            IKDG_RANGE(0, false);
         else
-            range_kernel<0, true><<<g, 128, 0, s>>>(t, q, q_stride, radius, nq, counts, offsets, ids, xyz);
+            IKDG_RANGE(0, true);
     } else {
         if (ids == nullptr)
-            range_kernel<1, false><<<g, 128, 0, s>>>(t, q, q_stride, radius, nq, counts, offsets, ids, xyz);
+            IKDG_RANGE(1, false);
         else
-            range_kernel<1, true><<<g, 128, 0, s>>>(t, q, q_stride, radius, nq, counts, offsets, ids, xyz);
+            IKDG_RANGE(1, true);
     }
+#undef IKDG_RANGE
 }
 
 }  // namespace ikdg

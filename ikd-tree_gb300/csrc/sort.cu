@@ -18,11 +18,12 @@ constexpr int SORT_ROUNDS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ROUNDS;  // 4096
 constexpr int RADIX = 256;
 
-__device__ __forceinline__ int warp_incl_scan(int v) {
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v) {
     int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, v, o);
+        T t = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += t;
     }
     return v;
@@ -30,47 +31,49 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
 // prefix and writes the block total into *total.
-template <int THREADS>
-__device__ __forceinline__ int block_excl_scan(int v, int* total) {
-    __shared__ int warp_sums[THREADS / 32];
+template <int THREADS, typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* total) {
+    __shared__ T warp_sums[THREADS / 32];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int inc = warp_incl_scan(v);
+    T inc = warp_incl_scan(v);
     if (lane == 31) warp_sums[w] = inc;
     __syncthreads();
     if (w == 0) {
-        int s = lane < THREADS / 32 ? warp_sums[lane] : 0;
-        int si = warp_incl_scan(s);
+        T s = lane < THREADS / 32 ? warp_sums[lane] : T(0);
+        T si = warp_incl_scan(s);
         if (lane < THREADS / 32) warp_sums[lane] = si - s;
         if (lane == THREADS / 32 - 1) *total = si;
     }
     __syncthreads();
-    int r = inc - v + warp_sums[w];
+    T r = inc - v + warp_sums[w];
     __syncthreads();
     return r;
 }
 
-__global__ void scan_reduce_kernel(const int* __restrict__ in, long long n, int* __restrict__ partial) {
+template <typename T>
+__global__ void scan_reduce_kernel(const T* __restrict__ in, long long n, T* __restrict__ partial) {
     long long base = (long long)blockIdx.x * SCAN_TILE;
-    int s = 0;
+    T s = 0;
     for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) {
         long long g = base + i;
         if (g < n) s += in[g];
     }
-    __shared__ int tot;
+    __shared__ T tot;
     block_excl_scan<SCAN_THREADS>(s, &tot);
     if (threadIdx.x == 0) partial[blockIdx.x] = tot;
 }
 
 // Single block: exclusive scan of the tile partials.
-__global__ void scan_partials_kernel(int* partial, int ntiles, int* total) {
-    __shared__ int carry;
+template <typename T>
+__global__ void scan_partials_kernel(T* partial, int ntiles, T* total) {
+    __shared__ T carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (int base = 0; base < ntiles; base += 1024) {
         int i = base + threadIdx.x;
-        int v = i < ntiles ? partial[i] : 0;
-        __shared__ int tot;
-        int ex = block_excl_scan<1024>(v, &tot);
+        T v = i < ntiles ? partial[i] : T(0);
+        __shared__ T tot;
+        T ex = block_excl_scan<1024>(v, &tot);
         if (i < ntiles) partial[i] = ex + carry;
         __syncthreads();
         if (threadIdx.x == 0) carry += tot;
@@ -79,24 +82,25 @@ __global__ void scan_partials_kernel(int* partial, int ntiles, int* total) {
     if (threadIdx.x == 0 && total != nullptr) *total = carry;
 }
 
-__global__ void scan_down_kernel(const int* __restrict__ in, int* __restrict__ out, long long n,
-                                 const int* __restrict__ partial) {
-    __shared__ int tile[SCAN_TILE];
+template <typename T>
+__global__ void scan_down_kernel(const T* __restrict__ in, T* __restrict__ out, long long n,
+                                 const T* __restrict__ partial) {
+    __shared__ T tile[SCAN_TILE];
     long long base = (long long)blockIdx.x * SCAN_TILE;
     for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) {
         long long g = base + i;
-        tile[i] = g < n ? in[g] : 0;
+        tile[i] = g < n ? in[g] : T(0);
     }
     __syncthreads();
-    int local[SCAN_ITEMS];
-    int s = 0;
+    T local[SCAN_ITEMS];
+    T s = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) {
         local[j] = s;
         s += tile[threadIdx.x * SCAN_ITEMS + j];
     }
-    __shared__ int tot;
-    int ex = block_excl_scan<SCAN_THREADS>(s, &tot) + partial[blockIdx.x];
+    __shared__ T tot;
+    T ex = block_excl_scan<SCAN_THREADS>(s, &tot) + partial[blockIdx.x];
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) tile[threadIdx.x * SCAN_ITEMS + j] = local[j] + ex;
     __syncthreads();
@@ -104,6 +108,19 @@ __global__ void scan_down_kernel(const int* __restrict__ in, int* __restrict__ o
         long long g = base + i;
         if (g < n) out[g] = tile[i];
     }
+}
+
+template <typename T>
+void exclusive_scan_t(const T* in, T* out, long long n, T* total, void* temp, cudaStream_t s) {
+    if (n <= 0) {
+        if (total) cudaMemsetAsync(total, 0, sizeof(T), s);
+        return;
+    }
+    int tiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+    T* partial = (T*)temp;
+    scan_reduce_kernel<T><<<tiles, SCAN_THREADS, 0, s>>>(in, n, partial);
+    scan_partials_kernel<T><<<1, 1024, 0, s>>>(partial, tiles, total);
+    scan_down_kernel<T><<<tiles, SCAN_THREADS, 0, s>>>(in, out, n, partial);
 }
 
 // ---- radix sort --------------------------------------------------------------
@@ -182,19 +199,15 @@ inline int ceil_div_ll(long long a, long long b) { return (int)((a + b - 1) / b)
 
 size_t scan_temp_bytes(long long n) {
     long long tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
-    return (size_t)((tiles + 64) * sizeof(int) + 256);
+    return (size_t)((tiles + 64) * sizeof(long long) + 256);
 }
 
 void exclusive_scan(const int* in, int* out, long long n, int* total, void* temp, cudaStream_t s) {
-    if (n <= 0) {
-        if (total) cudaMemsetAsync(total, 0, sizeof(int), s);
-        return;
-    }
-    int tiles = ceil_div_ll(n, SCAN_TILE);
-    int* partial = (int*)temp;
-    scan_reduce_kernel<<<tiles, SCAN_THREADS, 0, s>>>(in, n, partial);
-    scan_partials_kernel<<<1, 1024, 0, s>>>(partial, tiles, total);
-    scan_down_kernel<<<tiles, SCAN_THREADS, 0, s>>>(in, out, n, partial);
+    exclusive_scan_t<int>(in, out, n, total, temp, s);
+}
+
+void exclusive_scan(const long long* in, long long* out, long long n, long long* total, void* temp, cudaStream_t s) {
+    exclusive_scan_t<long long>(in, out, n, total, temp, s);
 }
 
 size_t sort_temp_bytes(long long n, int batch) {

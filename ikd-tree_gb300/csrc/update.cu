@@ -18,6 +18,8 @@
 //     [1 - alpha_bal, alpha_bal] is rebuilt, topmost first.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "update.cuh"
 
 namespace ikdg {
@@ -144,9 +146,13 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             atomicOr(&t.st->err, ERR_LOOP);
             return;
         }
+        // pend[X] is read before arriving: it cannot change until every
+        // walker has arrived (the last one resets it), whereas after the
+        // arrival the last walker may already have reset it to 0.
+        const int expect = __ldcg(&a.pend[X]);
         __threadfence();  // release: this walker's writes into X's record
         int old = atomicAdd(&a.arrive[X], 1);
-        if (old + 1 < __ldcg(&a.pend[X])) return;
+        if (old + 1 < expect) return;
         __threadfence();  // acquire: the other children's writes are visible
         a.pend[X] = 0;
         a.arrive[X] = 0;
@@ -204,6 +210,9 @@ __global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
         if (a.viol_flag[X]) return;  // an ancestor is rebuilt instead
         X = t.nparent[X] >> 1;
     }
+    // One job per subtree even if the violator was listed twice.
+    int* tag = code < 0 ? &a.job_of_leaf[code_leaf(code)] : &a.job_of_node[code];
+    if (atomicCAS(tag, -1, -2) != -1) return;
     int j = atomicAdd(&t.st->n_jobs, 1);
     if (j >= a.list_cap) {
         atomicOr(&t.st->err, ERR_LIST);
@@ -374,21 +383,78 @@ __global__ void job_finish_kernel(DevTree t, UpdateAux a, const int* n_jobs) {
 // ---- box / point deletion, box re-insertion ----------------------------------------
 
 constexpr int DB_THREADS = 128;
+constexpr int DB_WARPS = DB_THREADS / 32;
 constexpr int DB_STACK = DB_THREADS * (MAX_STACK + 2);
+constexpr int DB_SPLIT_BITS_MAX = 6;
+constexpr long long DB_TARGET_UNITS = 1024;
 
-// One CTA per box.  The CTA expands its share of the subtree cooperatively: each
-// round pops up to DB_THREADS items off a shared stack, and each thread either
-// expands a node (pushing the children that overlap the box, tagged when fully
-// covered) or processes a leaf.  MODE 0 deletes (flags |= del_flags), MODE 1
-// restores box-deleted points (Add_by_range).
+// Whether child `side` of node record r (code: its index, 0 = sentinel) can
+// hold points that box qb edits.  MODE 0 prunes by the child's AABB (which
+// bounds valid points) and reports full cover in ccov; MODE 1 looks for
+// deleted points, which only the split planes bound: the left subtree holds
+// coordinates <= split, the right >= split.
+template <int MODE>
+__device__ __forceinline__ bool box_child(const Box3& qb, const NodeRec& r, int code, int side, bool cov,
+                                          bool& ccov) {
+    ccov = cov;
+    if (MODE == 0) {
+        Box3 b = r.box(side);
+        if (box_empty(b)) return false;
+        if (!ccov) {
+            if (qbox_disjoint(qb, b)) return false;
+            ccov = qbox_covers(qb, b);
+        }
+    } else if (code > 0) {
+        int ax = r.axis();
+        float sp = r.split();
+        if (side == 0 && sp < qb.lo[ax]) return false;
+        if (side == 1 && qb.hi[ax] <= sp) return false;
+    }
+    return true;
+}
+
+// Work unit (box bi, part): the CTA walks split_bits levels down from the
+// root, taking the side that bit d of `part` names at depth d, and edits the
+// subtree it reaches.  A leaf met above that depth belongs to the part whose
+// remaining bits are zero.  Returns the stack item (code * 2 + covered) or
+// INT_MIN when the walk was pruned.
+template <int MODE>
+__device__ int box_seed(const DevTree& t, const Box3& qb, int part, int split_bits) {
+    NodeRec r = load_node_cg(t.node, 0);
+    int code = r.left();
+    bool cov = false, ccov;
+    if (code == 0 || !box_child<MODE>(qb, r, 0, 0, cov, ccov)) return INT_MIN;
+    cov = ccov;
+    for (int d = 0; d < split_bits; ++d) {
+        if (code < 0) return (part >> d) == 0 ? code * 2 + (cov ? 1 : 0) : INT_MIN;
+        r = load_node_cg(t.node, code);
+        int side = (part >> d) & 1;
+        int c = side == 0 ? r.left() : r.right();
+        if (c == 0 || !box_child<MODE>(qb, r, code, side, cov, ccov)) return INT_MIN;
+        code = c;
+        cov = ccov;
+    }
+    return code * 2 + (cov ? 1 : 0);
+}
+
+// One CTA per work unit (box, top-level subtree).  Each round the CTA pops up
+// to DB_THREADS items off a shared stack; threads expand nodes (pushing the
+// children that overlap the box, tagged when fully covered) and queue leaves,
+// then each warp edits queued leaves one slot per lane.  MODE 0 deletes
+// (flags |= del_flags), MODE 1 restores box-deleted points (Add_by_range).
 template <int MODE>
 __global__ void __launch_bounds__(DB_THREADS) box_edit_kernel(DevTree t, UpdateAux a, const float* __restrict__ boxes,
-                                                              long long m, uint32_t del_flags,
+                                                              long long m, int split_bits, uint32_t del_flags,
                                                               long long* __restrict__ total) {
     __shared__ int stack[DB_STACK];
-    __shared__ int top;
+    __shared__ int leafq[2 * DB_THREADS];
+    __shared__ int top, nleaf;
     __shared__ long long block_cnt;
-    for (long long bi = blockIdx.x; bi < m; bi += gridDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long units = m << split_bits;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        const long long bi = u >> split_bits;
+        const int part = (int)(u & ((1 << split_bits) - 1));
         Box3 qb;
         for (int k = 0; k < 3; ++k) {
             qb.lo[k] = boxes[bi * 6 + k];
@@ -396,8 +462,10 @@ __global__ void __launch_bounds__(DB_THREADS) box_edit_kernel(DevTree t, UpdateA
         }
         if (threadIdx.x == 0) {
             top = 0;
+            nleaf = 0;
             block_cnt = 0;
-            stack[top++] = 0 * 2;  // the sentinel record
+            int seed = box_seed<MODE>(t, qb, part, split_bits);
+            if (seed != INT_MIN) stack[top++] = seed;
         }
         __syncthreads();
         long long my_cnt = 0;
@@ -421,58 +489,55 @@ __global__ void __launch_bounds__(DB_THREADS) box_edit_kernel(DevTree t, UpdateA
                     NodeRec r = load_node_cg(t.node, code);
                     for (int side = 0; side < 2; ++side) {
                         int c = side == 0 ? r.left() : r.right();
-                        if (c == 0) continue;
-                        Box3 b = r.box(side);
-                        bool ccov = cov;
-                        if (MODE == 0) {
-                            if (box_empty(b)) continue;
-                            if (!ccov) {
-                                if (qbox_disjoint(qb, b)) continue;
-                                ccov = qbox_covers(qb, b);
-                            }
-                        } else if (code > 0) {
-                            // AABBs bound valid points only; deleted points are
-                            // bounded by the split planes instead: the left
-                            // subtree holds coordinates <= split, the right >= split.
-                            int ax = r.axis();
-                            float sp = r.split();
-                            if (side == 0 && sp < qb.lo[ax]) continue;
-                            if (side == 1 && qb.hi[ax] <= sp) continue;
+                        bool ccov;
+                        if (c == 0 || !box_child<MODE>(qb, r, code, side, cov, ccov)) continue;
+                        int it = c * 2 + (ccov ? 1 : 0);
+                        if (c < 0) {
+                            leafq[atomicAdd(&nleaf, 1)] = it;  // <= 2 per thread
+                        } else {
+                            int pos = atomicAdd(&top, 1);
+                            if (pos < DB_STACK)
+                                stack[pos] = it;
+                            else
+                                atomicOr(&t.st->err, ERR_STACK);
                         }
-                        int pos = atomicAdd(&top, 1);
-                        if (pos < DB_STACK)
-                            stack[pos] = c * 2 + (ccov ? 1 : 0);
-                        else
-                            atomicOr(&t.st->err, ERR_STACK);
                     }
                 } else {
-                    int L = code_leaf(code);
-                    int nl = t.leaf_n[L];
-                    int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
-                    float4* lp = t.pts + (long long)L * LEAF_CAP;
-                    bool any = false;
-                    for (int s = 0; s < ml; ++s) {
-                        float4 p = __ldcg(lp + s);
-                        uint32_t w = __float_as_uint(p.w);
-                        if (MODE == 0) {
-                            if (w & F_DEL) continue;
-                            if (!cov && !qbox_holds(qb, p.x, p.y, p.z)) continue;
-                            unsigned old = atomicOr((unsigned*)&lp[s].w, del_flags);
-                            if (!(old & F_DEL)) {
-                                ++my_cnt;
-                                any = true;
-                            }
-                        } else {
-                            if (!(w & F_DEL) || (w & F_DSDEL)) continue;
-                            if (!cov && !qbox_holds(qb, p.x, p.y, p.z)) continue;
-                            atomicAnd((unsigned*)&lp[s].w, ~F_DEL);
-                            any = true;
-                        }
-                    }
-                    if (any) mark_dirty(a, t.st, L);
+                    leafq[atomicAdd(&nleaf, 1)] = item;
                 }
             }
             __syncthreads();
+            const int nq = nleaf;
+            for (int q = warp; q < nq; q += DB_WARPS) {
+                const int it = leafq[q];
+                const int L = code_leaf(it >> 1);
+                const bool cov = it & 1;
+                const int nl = t.leaf_n[L];
+                float4* lp = t.pts + (long long)L * LEAF_CAP;
+                bool hit = false;
+                if (lane < nl && lane < LEAF_CAP) {
+                    float4 p = __ldcg(lp + lane);
+                    uint32_t w = __float_as_uint(p.w);
+                    if (MODE == 0) {
+                        if (!(w & F_DEL) && (cov || qbox_holds(qb, p.x, p.y, p.z))) {
+                            unsigned old = atomicOr((unsigned*)&lp[lane].w, del_flags);
+                            hit = !(old & F_DEL);
+                        }
+                    } else {
+                        if ((w & F_DEL) && !(w & F_DSDEL) && (cov || qbox_holds(qb, p.x, p.y, p.z))) {
+                            atomicAnd((unsigned*)&lp[lane].w, ~F_DEL);
+                            hit = true;
+                        }
+                    }
+                }
+                unsigned bal = __ballot_sync(0xffffffffu, hit);
+                if (bal && lane == 0) {
+                    mark_dirty(a, t.st, L);
+                    my_cnt += __popc(bal);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) nleaf = 0;
         }
         if (MODE == 0 && my_cnt) atomicAdd((unsigned long long*)&block_cnt, (unsigned long long)my_cnt);
         __syncthreads();
@@ -480,6 +545,16 @@ __global__ void __launch_bounds__(DB_THREADS) box_edit_kernel(DevTree t, UpdateA
         __syncthreads();
     }
 }
+
+// Subtree split for box edits: enough (box, subtree) units to fill the GPU
+// when there are few boxes, none when there are many.
+int box_split_bits(long long m) {
+    int bits = 0;
+    while (bits < DB_SPLIT_BITS_MAX && (m << bits) < DB_TARGET_UNITS) ++bits;
+    return bits;
+}
+
+unsigned box_grid(long long units) { return (unsigned)(units < (1LL << 20) ? units : (1LL << 20)); }
 
 // same_point (ikd_Tree.cpp:1368-1371): |a - b| < 1e-6 per axis, the float
 // difference compared in double.
@@ -598,7 +673,7 @@ __device__ __forceinline__ void note_bad(DevStatus* st, int kind, int X, int sid
 
 // For every live node: both children exist and point back; the child box and
 // counts stored in the node equal what the child itself holds.
-__global__ void validate_nodes_kernel(DevTree t, unsigned long long* bad) {
+__global__ void validate_nodes_kernel(DevTree t, bool at_rest, unsigned long long* bad) {
     int X = blockIdx.x * blockDim.x + threadIdx.x;
     if (X >= t.st->node_top) return;
     if (X > 0 && t.nparent[X] < 0) return;
@@ -646,13 +721,16 @@ __global__ void validate_nodes_kernel(DevTree t, unsigned long long* bad) {
                 continue;
             }
             int n = t.leaf_n[L];
-            if (n > LEAF_CAP || n < 0) {
+            // Between a refit and its rebuild jobs a leaf may hold more
+            // points than slots (its overflow is queued for the rebuild).
+            if ((n > LEAF_CAP && at_rest) || n < 0) {
                 ++nbad;
                 note_bad(t.st, 105, X, side, c, n, 0, 0);
                 continue;
             }
             s2 = n;
-            for (int j = 0; j < n; ++j) {
+            const int m = n < LEAF_CAP ? n : LEAF_CAP;
+            for (int j = 0; j < m; ++j) {
                 float4 p = __ldcg(t.pts + (long long)L * LEAF_CAP + j);
                 if (__float_as_uint(p.w) & F_DEL)
                     ++d2;
@@ -691,6 +769,30 @@ __global__ void validate_leaves_kernel(DevTree t, unsigned long long* bad) {
     if (!ok) {
         atomicAdd(bad, 1ull);
         note_bad(t.st, 108, P, lp & 1, L, lp, 0, 0);
+    }
+}
+
+// Refit / rebuild bookkeeping that must be clear between refits (arrival
+// counters) or between calls (violation and job tags, dirty flags).
+__global__ void validate_aux_nodes_kernel(DevTree t, UpdateAux a, bool at_rest, unsigned long long* bad) {
+    int X = blockIdx.x * blockDim.x + threadIdx.x;
+    if (X >= t.node_cap) return;
+    if (a.pend[X] != 0 || a.arrive[X] != 0) {
+        atomicAdd(bad, 1ull);
+        note_bad(t.st, 109, X, a.pend[X], a.arrive[X], X < t.st->node_top ? t.nparent[X] : -9, 0, 0);
+    }
+    if (at_rest && (a.viol_flag[X] != 0 || a.job_of_node[X] != -1)) {
+        atomicAdd(bad, 1ull);
+        note_bad(t.st, 110, X, a.viol_flag[X], a.job_of_node[X], 0, 0, 0);
+    }
+}
+
+__global__ void validate_aux_leaves_kernel(DevTree t, UpdateAux a, unsigned long long* bad) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= t.leaf_cap) return;
+    if (a.dirty_flag[L] != 0 || a.job_of_leaf[L] != -1) {
+        atomicAdd(bad, 1ull);
+        note_bad(t.st, 111, L, a.dirty_flag[L], a.job_of_leaf[L], L < t.st->leaf_top ? t.lparent[L] : -9, 0, 0);
     }
 }
 
@@ -1091,14 +1193,14 @@ void launch_job_finish(const DevTree& t, const UpdateAux& a, int max_jobs, cudaS
 void launch_delete_boxes(const DevTree& t, const UpdateAux& a, const float* boxes, long long m, uint32_t flags,
                          long long* total, cudaStream_t s) {
     if (m <= 0) return;
-    unsigned g = (unsigned)(m < 65535 ? m : 65535);
-    box_edit_kernel<0><<<g, DB_THREADS, 0, s>>>(t, a, boxes, m, flags, total);
+    int bits = box_split_bits(m);
+    box_edit_kernel<0><<<box_grid(m << bits), DB_THREADS, 0, s>>>(t, a, boxes, m, bits, flags, total);
 }
 
 void launch_add_boxes(const DevTree& t, const UpdateAux& a, const float* boxes, long long m, cudaStream_t s) {
     if (m <= 0) return;
-    unsigned g = (unsigned)(m < 65535 ? m : 65535);
-    box_edit_kernel<1><<<g, DB_THREADS, 0, s>>>(t, a, boxes, m, 0u, nullptr);
+    int bits = box_split_bits(m);
+    box_edit_kernel<1><<<box_grid(m << bits), DB_THREADS, 0, s>>>(t, a, boxes, m, bits, 0u, nullptr);
 }
 
 void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts, int stride, long long n,
@@ -1109,11 +1211,15 @@ void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts
 
 void launch_snapshot_root(const DevTree& t, cudaStream_t s) { snapshot_root_kernel<<<1, 1, 0, s>>>(t); }
 
-void launch_validate(const DevTree& t, long long* bad, cudaStream_t s) {
+void launch_validate(const DevTree& t, const UpdateAux& a, bool at_rest, long long* bad, cudaStream_t s) {
     if (t.node_cap > 0)
-        validate_nodes_kernel<<<blocks_for(t.node_cap, 256), 256, 0, s>>>(t, (unsigned long long*)bad);
+        validate_nodes_kernel<<<blocks_for(t.node_cap, 256), 256, 0, s>>>(t, at_rest, (unsigned long long*)bad);
     if (t.leaf_cap > 0)
         validate_leaves_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, (unsigned long long*)bad);
+    if (t.node_cap > 0)
+        validate_aux_nodes_kernel<<<blocks_for(t.node_cap, 256), 256, 0, s>>>(t, a, at_rest, (unsigned long long*)bad);
+    if (t.leaf_cap > 0)
+        validate_aux_leaves_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, a, (unsigned long long*)bad);
 }
 
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s) {

@@ -68,7 +68,10 @@ void launch_check_finite(const DevTree& t, const float* in, long long count, cud
 // Copies every valid point ({x, y, z, id}) to out; *counter += count.
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s);
 // Structural check of the whole tree; *bad += number of violations.
-void launch_validate(const DevTree& t, long long* bad, cudaStream_t s);
+// Structural check (links, counts, AABBs) plus the bookkeeping flags; at_rest
+// (between calls) also requires cleared violation / job tags and leaves within
+// their slots.
+void launch_validate(const DevTree& t, const UpdateAux& a, bool at_rest, long long* bad, cudaStream_t s);
 // Makes the whole tree the single rebuild job (st->n_jobs = 1).
 void launch_select_root_job(const DevTree& t, const UpdateAux& a, cudaStream_t s);
 

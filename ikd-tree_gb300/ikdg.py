@@ -64,6 +64,25 @@ SIGNATURES = {
     "ikdg_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "ikdg_set_stream": (C.c_int, [_vp, _vp]),
     "ikdg_synchronize": (C.c_int, [_vp]),
+    "ikdg_box_search_device": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, _vp, C.c_int64, _vp]),
+    "ikdg_radius_search_device": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, _vp, C.c_int32, _vp, _vp, _vp,
+                                            C.c_int64, _vp]),
+    "ikdg_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "ikdg_batch_destroy": (C.c_int, [_vp]),
+    "ikdg_batch_clear": (C.c_int, [_vp]),
+    "ikdg_batch_last_error": (C.c_char_p, [_vp]),
+    "ikdg_batch_add_knn": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int32, C.c_int32, C.c_double, _vp, _vp, _vp,
+                                     _vp, _ip]),
+    "ikdg_batch_add_box_search": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, C.c_int64, _ip]),
+    "ikdg_batch_add_radius_search": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int32, _vp, C.c_int32, _vp, _vp,
+                                               _vp, C.c_int64, _ip]),
+    "ikdg_batch_set_knn_lanes": (C.c_int, [_vp, C.c_int32, C.c_int32]),
+    "ikdg_batch_set_graph": (C.c_int, [_vp, C.c_int]),
+    "ikdg_batch_run": (C.c_int, [_vp]),
+    "ikdg_batch_synchronize": (C.c_int, [_vp, _lp]),
+    "ikdg_batch_autotune": (C.c_int, [_vp, C.c_int32, _ip]),
+    "ikdg_batch_num_trees": (C.c_int, [_vp, _ip]),
+    "ikdg_batch_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
 }
 
 _lib = None
@@ -352,3 +371,113 @@ class KDTree:
         self._check(self.lib.ikdg_knn_device(self.h, _vp(q_ptr), nq, stride, k, float(max_dist), _vp(ids_ptr),
                                              _vp(d2_ptr), _vp(xyz_ptr or None), _vp(cnt_ptr or None)),
                     "knn_device")
+
+    def box_search_device(self, boxes_ptr: int, nb: int, offsets_ptr: int, ids_ptr: int, capacity: int,
+                          xyz_ptr: int = 0, total_ptr: int = 0):
+        """Box_Search over device buffers (CSR), asynchronous on the tree's stream."""
+        self._check(self.lib.ikdg_box_search_device(self.h, _vp(boxes_ptr or None), nb, _vp(offsets_ptr),
+                                                    _vp(ids_ptr or None), _vp(xyz_ptr or None), capacity,
+                                                    _vp(total_ptr or None)), "box_search_device")
+
+    def radius_search_device(self, centers_ptr: int, nq: int, radius_ptr: int, offsets_ptr: int, ids_ptr: int,
+                             capacity: int, xyz_ptr: int = 0, total_ptr: int = 0, stride: int = 3,
+                             radius_stride: int = 1):
+        """Radius_Search over device buffers (CSR), asynchronous on the tree's stream."""
+        self._check(self.lib.ikdg_radius_search_device(self.h, _vp(centers_ptr or None), nq, stride,
+                                                       _vp(radius_ptr or None), radius_stride, _vp(offsets_ptr),
+                                                       _vp(ids_ptr or None), _vp(xyz_ptr or None), capacity,
+                                                       _vp(total_ptr or None)), "radius_search_device")
+
+
+class Batch:
+    """Many searches over many trees, run as one CUDA graph (see ikdg.h).
+
+    Requests take device pointers (e.g. ``tensor.data_ptr()``) that must stay
+    valid while the batch holds them."""
+
+    def __init__(self, device: int = -1):
+        self.lib = load()
+        h = _vp()
+        st = self.lib.ikdg_batch_create(device, C.byref(h))
+        if st != OK:
+            raise IkdgError(st, self.lib.ikdg_status_string(st).decode())
+        self.h = h
+        self._keep = []  # trees referenced by requests
+
+    def _check(self, st: int, what: str):
+        if st != OK:
+            msg = self.lib.ikdg_batch_last_error(self.h).decode() if self.h else ""
+            raise IkdgError(st, f"{what}: {self.lib.ikdg_status_string(st).decode()} ({msg})")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ikdg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clear(self):
+        self._check(self.lib.ikdg_batch_clear(self.h), "batch_clear")
+        self._keep = []
+
+    def add_knn(self, tree: KDTree, q_ptr: int, nq: int, k: int, max_dist: float, ids_ptr: int, d2_ptr: int,
+                xyz_ptr: int = 0, cnt_ptr: int = 0, stride: int = 3) -> int:
+        r = C.c_int32()
+        self._check(self.lib.ikdg_batch_add_knn(self.h, tree.h, _vp(q_ptr or None), nq, stride, k, float(max_dist),
+                                                _vp(ids_ptr or None), _vp(d2_ptr or None), _vp(xyz_ptr or None),
+                                                _vp(cnt_ptr or None), C.byref(r)), "batch_add_knn")
+        self._keep.append(tree)
+        return r.value
+
+    def add_box_search(self, tree: KDTree, boxes_ptr: int, nb: int, offsets_ptr: int, ids_ptr: int, capacity: int,
+                       xyz_ptr: int = 0) -> int:
+        r = C.c_int32()
+        self._check(self.lib.ikdg_batch_add_box_search(self.h, tree.h, _vp(boxes_ptr or None), nb, _vp(offsets_ptr),
+                                                       _vp(ids_ptr or None), _vp(xyz_ptr or None), capacity,
+                                                       C.byref(r)), "batch_add_box_search")
+        self._keep.append(tree)
+        return r.value
+
+    def add_radius_search(self, tree: KDTree, centers_ptr: int, nq: int, radius_ptr: int, offsets_ptr: int,
+                          ids_ptr: int, capacity: int, xyz_ptr: int = 0, stride: int = 3,
+                          radius_stride: int = 1) -> int:
+        r = C.c_int32()
+        self._check(self.lib.ikdg_batch_add_radius_search(self.h, tree.h, _vp(centers_ptr or None), nq, stride,
+                                                          _vp(radius_ptr or None), radius_stride, _vp(offsets_ptr),
+                                                          _vp(ids_ptr or None), _vp(xyz_ptr or None), capacity,
+                                                          C.byref(r)), "batch_add_radius_search")
+        self._keep.append(tree)
+        return r.value
+
+    def set_knn_lanes(self, request: int, lanes: int):
+        self._check(self.lib.ikdg_batch_set_knn_lanes(self.h, request, lanes), "batch_set_knn_lanes")
+
+    def set_graph(self, use_graph: bool):
+        self._check(self.lib.ikdg_batch_set_graph(self.h, 1 if use_graph else 0), "batch_set_graph")
+
+    def run(self):
+        self._check(self.lib.ikdg_batch_run(self.h), "batch_run")
+
+    def synchronize(self, n_range: int = 0) -> np.ndarray:
+        """Waits for the last run; returns the totals of the range requests."""
+        tot = np.zeros(max(n_range, 1), np.int64)
+        self._check(self.lib.ikdg_batch_synchronize(self.h, tot.ctypes.data_as(_lp)), "batch_synchronize")
+        return tot[:n_range]
+
+    def autotune(self, reps: int = 3) -> np.ndarray:
+        """Picks leaf fill and kNN lanes per tree; returns {fill, lanes} rows."""
+        n = C.c_int32()
+        self._check(self.lib.ikdg_batch_num_trees(self.h, C.byref(n)), "batch_num_trees")
+        out = np.zeros((max(n.value, 1), 2), np.int32)
+        self._check(self.lib.ikdg_batch_autotune(self.h, reps, out.ctypes.data_as(_ip)), "batch_autotune")
+        return out[:n.value]
+
+    @property
+    def stream(self) -> int:
+        s = _vp()
+        self._check(self.lib.ikdg_batch_get_stream(self.h, C.byref(s)), "batch_get_stream")
+        return s.value or 0

@@ -11,7 +11,11 @@ float32, with the shapes and distributions the configurations name.
   -15..+15 deg, 625 azimuth steps, range 1-100 m) ray-cast against the same
   geometry along a 1 m/scan random walk;
 * the sliding-window deletion of that workflow: the complement of a cube
-  around the pose as at most six slab boxes.
+  around the pose as at most six slab boxes;
+* many independent maps with mixed kNN / box / radius query batches (the
+  batched multi-map workload);
+* a large map: uniform points in a flat slab plus planar clusters (the scale
+  stress workload).
 """
 from __future__ import annotations
 
@@ -128,3 +132,86 @@ def cube_complement_boxes(center, half: float) -> np.ndarray:
     b.append([lo[0], lo[1], -BIG, hi[0], hi[1], lo[2]])     # z < lo
     b.append([lo[0], lo[1], hi[2], hi[0], hi[1], BIG])      # z >= hi
     return np.asarray(b, F32)
+
+
+@dataclass
+class MapRequests:
+    """One map of the multi-map workload and its three query batches."""
+    points: np.ndarray     # [N, 3]
+    knn_q: np.ndarray      # [nk, 3]
+    k: int
+    max_dist: float
+    boxes: np.ndarray      # [nb, 6] {min xyz, max xyz}
+    radius_q: np.ndarray   # [nr, 3]
+    radius: np.ndarray     # [nr]
+
+
+def multi_maps(seed: int, n_maps: int = 64, size_range=(1e4, 1e6), query_range=(1e3, 1e5),
+               side_range=(20.0, 200.0), kmax: int = 16) -> list[MapRequests]:
+    """Independent maps with sizes log-uniform in size_range, each uniform in
+    its own AABB (sides uniform in side_range); per map a query batch of
+    log-uniform size split 60 % kNN (k uniform in 1..kmax, max_dist uniform in
+    1-10 m), 20 % cubic boxes (side uniform in 0.5-5 m), 20 % radius queries
+    (r uniform in 0.5-5 m), all centred uniformly in the map's AABB."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_maps):
+        n = int(round(math.exp(rng.uniform(math.log(size_range[0]), math.log(size_range[1])))))
+        sides = rng.uniform(side_range[0], side_range[1], 3)
+        lo = rng.uniform(-500.0, 500.0, 3)
+        pts = (lo + rng.uniform(0.0, 1.0, (n, 3)) * sides).astype(F32)
+        nq = int(round(math.exp(rng.uniform(math.log(query_range[0]), math.log(query_range[1])))))
+        nk = int(round(0.6 * nq))
+        nb = int(round(0.2 * nq))
+        nr = nq - nk - nb
+
+        def centres(m):
+            return (lo + rng.uniform(0.0, 1.0, (m, 3)) * sides).astype(F32)
+
+        kq = centres(nk)
+        k = int(rng.integers(1, kmax + 1))
+        max_dist = float(rng.uniform(1.0, 10.0))
+        bc = centres(nb)
+        half = (rng.uniform(0.5, 5.0, nb) / 2.0).astype(F32)[:, None]
+        boxes = np.concatenate([bc - half, bc + half], axis=1).astype(F32)
+        rq = centres(nr)
+        rad = rng.uniform(0.5, 5.0, nr).astype(F32)
+        out.append(MapRequests(pts, kq, k, max_dist, boxes, rq, rad))
+    return out
+
+
+def stress_map(n: int, seed: int, n_clusters: int = 400, cluster_frac: float = 0.3) -> np.ndarray:
+    """Uniform points in [-500, 500]^2 x [0, 50] m plus planar clusters: a
+    fraction of the points lies on random planar patches (10-60 m wide
+    rectangles at random orientation, 2 cm noise)."""
+    rng = np.random.default_rng(seed)
+    nc = int(n * cluster_frac)
+    nu = n - nc
+    u = np.empty((nu, 3), F32)
+    u[:, 0:2] = rng.uniform(-500.0, 500.0, (nu, 2))
+    u[:, 2] = rng.uniform(0.0, 50.0, nu)
+    which = rng.integers(0, n_clusters, nc)
+    centre = np.stack([rng.uniform(-500, 500, n_clusters), rng.uniform(-500, 500, n_clusters),
+                       rng.uniform(0, 50, n_clusters)], 1)
+    normal = rng.normal(size=(n_clusters, 3))
+    normal /= np.linalg.norm(normal, axis=1, keepdims=True)
+    a = np.cross(normal, np.array([0.0, 0.0, 1.0]))
+    bad = np.linalg.norm(a, axis=1) < 1e-6
+    a[bad] = np.cross(normal[bad], np.array([1.0, 0.0, 0.0]))
+    a /= np.linalg.norm(a, axis=1, keepdims=True)
+    b = np.cross(normal, a)
+    w = rng.uniform(10.0, 60.0, (n_clusters, 2))
+    s = rng.uniform(-0.5, 0.5, (nc, 2)) * w[which]
+    c = (centre[which] + s[:, :1] * a[which] + s[:, 1:] * b[which] +
+         rng.normal(0.0, 0.02, (nc, 1)) * normal[which])
+    return np.concatenate([u, c.astype(F32)])[rng.permutation(n)].astype(F32)
+
+
+def random_boxes(m: int, seed: int, side_range=(1.0, 20.0), lo=(-500.0, -500.0, 0.0),
+                 hi=(500.0, 500.0, 50.0)) -> np.ndarray:
+    """m axis-aligned boxes, centres uniform in [lo, hi], sides uniform in
+    side_range per axis."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(lo, hi, (m, 3))
+    h = rng.uniform(side_range[0], side_range[1], (m, 3)) / 2.0
+    return np.concatenate([c - h, c + h], axis=1).astype(F32)

@@ -33,6 +33,7 @@ extern "C" {
 #endif
 
 typedef struct ikdg_tree ikdg_tree;
+typedef struct ikdg_batch ikdg_batch;
 
 enum ikdg_status {
     IKDG_OK = 0,
@@ -137,6 +138,70 @@ int ikdg_box_search(ikdg_tree* t, const float* boxes, int64_t nb, int64_t* offse
 int ikdg_radius_search(ikdg_tree* t, const float* centers, int64_t nq, int32_t stride, const float* radius,
                        int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
                        int64_t* total);
+
+/* Device-pointer forms of ikdg_box_search / ikdg_radius_search (the reference
+ * has only the per-point host calls above): every pointer is a device pointer,
+ * the call is asynchronous on the tree's stream and never waits for the GPU.
+ * offsets (nq + 1 entries) and *total (nullable) are always written; a query
+ * whose hits would end past `capacity` writes no ids / xyz, so compare *total
+ * with capacity after synchronising.  Hits come in the same order as from the
+ * host-pointer calls. */
+int ikdg_box_search_device(ikdg_tree* t, const float* boxes, int64_t nb, int64_t* offsets, int32_t* ids, float* xyz,
+                           int64_t capacity, int64_t* total);
+int ikdg_radius_search_device(ikdg_tree* t, const float* centers, int64_t nq, int32_t stride, const float* radius,
+                              int32_t radius_stride, int64_t* offsets, int32_t* ids, float* xyz, int64_t capacity,
+                              int64_t* total);
+
+/* ---- Multi-tree batches (no counterpart in the reference) -------------------
+ * A batch is a list of search requests over any number of trees (same
+ * device), each with the semantics and results of the per-call device entry
+ * points (ikdg_knn_device, ikdg_box_search_device, ikdg_radius_search_device).
+ * ikdg_batch_run issues the whole list at once as one CUDA graph: the trees'
+ * descriptors are refreshed, one persistent search kernel per register class
+ * (kNN k <= 1, 2, 4, 8, 16 and box / radius) runs on its own graph branch, and
+ * box / radius requests then get a device prefix sum and one persistent write
+ * kernel.  The graph is built at the first run after requests change.
+ *
+ * All query / output pointers are device pointers owned by the caller; they
+ * must stay valid until the batch is cleared or destroyed, and their contents
+ * may change between runs (the graph reads them at run time).  Trees may be
+ * mutated between runs: a run waits for work already queued on each tree's
+ * stream, and later work on those streams waits for the run.  A tree must not
+ * be destroyed while a batch holds requests on it.  `request` (nullable)
+ * receives the request's index. */
+int ikdg_batch_create(int device, ikdg_batch** out);
+int ikdg_batch_destroy(ikdg_batch* b);
+int ikdg_batch_clear(ikdg_batch* b);
+const char* ikdg_batch_last_error(const ikdg_batch* b);
+/* kNN request, k <= 16; outputs as ikdg_knn. */
+int ikdg_batch_add_knn(ikdg_batch* b, ikdg_tree* t, const float* queries, int64_t nq, int32_t stride, int32_t k,
+                       double max_dist, int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count,
+                       int32_t* request);
+/* Box / radius requests: CSR output as ikdg_box_search_device, per request. */
+int ikdg_batch_add_box_search(ikdg_batch* b, ikdg_tree* t, const float* boxes, int64_t nb, int64_t* offsets,
+                              int32_t* ids, float* xyz, int64_t capacity, int32_t* request);
+int ikdg_batch_add_radius_search(ikdg_batch* b, ikdg_tree* t, const float* centers, int64_t nq, int32_t stride,
+                                 const float* radius, int32_t radius_stride, int64_t* offsets, int32_t* ids,
+                                 float* xyz, int64_t capacity, int32_t* request);
+/* Lanes per kNN query of one request (1, 2, 4; 0 = the tree's setting). */
+int ikdg_batch_set_knn_lanes(ikdg_batch* b, int32_t request, int32_t lanes);
+/* use_graph 0: issue the same kernels directly at every run (no graph). */
+int ikdg_batch_set_graph(ikdg_batch* b, int use_graph);
+/* Asynchronous on the batch's stream. */
+int ikdg_batch_run(ikdg_batch* b);
+/* Waits for the last run.  range_totals (nullable, host) receives one total
+ * per box / radius request, in the order they were added.  IKDG_CAPACITY when
+ * a request's hits exceeded its capacity (those queries wrote no ids). */
+int ikdg_batch_synchronize(ikdg_batch* b, int64_t* range_totals);
+/* Autotuner: per tree of the batch, times that tree's requests alone for
+ * every leaf fill in {8, 12, 16, 24, 32} (the tree is rebuilt at each) and
+ * every lanes-per-kNN-query in {1, 2, 4} (median of `reps` runs), then keeps
+ * the fastest pair: the tree stays rebuilt at that fill, its kNN requests get
+ * those lanes.  chosen (nullable, host) receives {fill, lanes} per distinct
+ * tree, in order of first use.  Results do not depend on either setting. */
+int ikdg_batch_autotune(ikdg_batch* b, int32_t reps, int32_t* chosen);
+int ikdg_batch_num_trees(ikdg_batch* b, int32_t* n);
+int ikdg_batch_get_stream(ikdg_batch* b, void** stream);
 
 /* Scan-to-map point-to-plane residuals on top of Nearest_Search (no
  * counterpart in the reference; the step its main consumer, FAST-LIO2, runs on
