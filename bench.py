@@ -305,6 +305,21 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
         for t in trees:
             t.synchronize()
 
+    def plain_sync():
+        # each request awaited before the next, as a caller consuming every
+        # result in turn (the reference's calls are synchronous)
+        for kind, t, r in reqs:
+            if kind == "knn":
+                t.knn_device(r["q"].data_ptr(), r["nq"], r["k"], r["md"], r["ids"].data_ptr(), r["d2"].data_ptr(),
+                             r["xyz"].data_ptr(), r["cnt"].data_ptr())
+            elif kind == "box":
+                t.box_search_device(r["q"].data_ptr(), r["nq"], r["offs"].data_ptr(), r["ids"].data_ptr(),
+                                    r["cap"], r["xyz"].data_ptr(), r["total"].data_ptr())
+            else:
+                t.radius_search_device(r["q"].data_ptr(), r["nq"], r["rad"].data_ptr(), r["offs"].data_ptr(),
+                                       r["ids"].data_ptr(), r["cap"], r["xyz"].data_ptr(), r["total"].data_ptr())
+            t.synchronize()
+
     b = ikdg.Batch(device)
     for kind, t, r in reqs:
         if kind == "knn":
@@ -345,6 +360,7 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
         return statistics.median(ts)
 
     plain_ms = timed(plain)
+    plain_sync_ms = timed(plain_sync)
     batch_ms = timed(batched)
     batch_dev = batch_device_ms()
     tuned = None
@@ -365,9 +381,14 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
                     "ids + points out; inputs larger than L2",
         "queries": n_queries,
         "plain_ms": plain_ms, "plain_queries_per_s": n_queries / (plain_ms / 1e3),
+        "plain": "per-call device entry points, asynchronous, each tree on its own stream (requests of "
+                 "different trees overlap); one wait at the end",
+        "plain_sync_ms": plain_sync_ms,
+        "plain_sync": "the same calls, each awaited before the next",
         "batched_ms": batch_ms, "batched_queries_per_s": n_queries / (batch_ms / 1e3),
         "batched_device_ms": batch_dev,
         "speedup_vs_plain": plain_ms / batch_ms,
+        "speedup_vs_plain_sync": plain_sync_ms / batch_ms,
         "autotuned": tuned,
         "plain_launches": 64 + n_range * 5,
         "timing": "host wall clock from issue to completion, median of %d runs" % reps,
@@ -547,7 +568,9 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": knn_traffic(), "peak_source": peak_kind,
                      "bytes_per_query": bytes_per_query(N_MAP, K)},
         "clocks": clocks,
-        "gpu_launches": 2 * Kst,
+        # one knn_kernel launch per timed step (query binning is off by
+        # default); the L2 flush between steps is a torch fill, not ours
+        "gpu_launches": Kst,
         "update_ms_per_scan": lidar["update_ms_per_scan"],
         "update": {"workload": f"lidar map {LIDAR_MAP} pts, {LIDAR_SCANS} scans of ~{lidar['scan_points']} pts, "
                                "0.5 m downsampling, 200 m sliding cube", **lidar},
@@ -566,6 +589,24 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_leg(args):
+    """One leg alone (for profiling): prints its JSON object."""
+    import torch
+    import ikdg
+    torch.cuda.set_device(0)
+    if args.leg == "lidar":
+        base, scans = lidar_workload()
+        t = ikdg.KDTree(0.5, 0.6, DS)
+        t.Build(base)
+        out = run_scans(t, scans, lambda p: t.knn(p, K, 5.0, want_xyz=True))
+        t.close()
+    elif args.leg == "batch":
+        out = multimap_bench(ikdg, torch, 0, reps=2, tune=False)
+    else:
+        out = stress_bench(ikdg, torch, 0, reps=1)
+    print(json.dumps({"leg": args.leg, **out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -575,8 +616,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the multi-map batch leg")
     ap.add_argument("--no-stress", action="store_true", help="skip the 20M-point scale leg")
+    ap.add_argument("--leg", choices=["lidar", "batch", "stress"], default=None,
+                    help="run one leg alone on GPU 0 (for profiling) and print its object")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.leg is not None:
+        run_leg(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

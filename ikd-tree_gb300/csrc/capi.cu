@@ -783,7 +783,7 @@ struct Tree {
     void p2p_forward(const float* scan, long long n, const double* pose, int k, double max_dist, float thresh,
                      float* planes, float* res, int* valid, double* loss) {
         if (n < 0 || scan == nullptr || pose == nullptr || planes == nullptr || res == nullptr || valid == nullptr ||
-            k < 3 || k > KNN_REG_MAX)
+            k < 3 || k > KNN_SMEM_MAX)
             throw BadArg{"p2p_forward: bad arguments"};
         if (loss) *loss = 0;
         if (n == 0) return;
@@ -1535,7 +1535,7 @@ int ikdg_knn_device_noalloc(ikdg_tree* h, const float* q, int64_t nq, int32_t st
     return guarded(h, [&](ikdg::Tree& t) {
         if (nq < 0 || stride < 3 || k < 1 || (nq > 0 && (q == nullptr || ids == nullptr || d2 == nullptr)))
             throw ikdg::BadArg{"knn_device_noalloc: bad arguments"};
-        if (k > ikdg::KNN_REG_MAX) throw ikdg::BadArg{"knn_device_noalloc: k must be <= 64"};
+        if (k > ikdg::KNN_SMEM_MAX) throw ikdg::BadArg{"knn_device_noalloc: k must be <= 64"};
         if (nq > ikdg::NOALLOC_MAX_QUERIES)
             throw ikdg::BadArg{"knn_device_noalloc: at most " + std::to_string(ikdg::NOALLOC_MAX_QUERIES) +
                                " queries per call (size of the static scratch array)"};

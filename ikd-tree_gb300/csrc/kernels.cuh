@@ -51,8 +51,14 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
 // Batched kNN.  `temp` must hold knn_temp_bytes(nq, k) bytes of device
 // scratch: the query binning (QBIN_BINS counters, a key and a permutation
 // entry per query, for batches of at least QBIN_MIN_QUERIES) and, for
-// k > KNN_REG_MAX, k slot indices per query.
-constexpr int KNN_REG_MAX = 64;
+// k > KNN_SMEM_MAX, k slot indices per query.  The candidate lists live in
+// registers for k <= KNN_REG_MAX, in shared memory for k <= KNN_SMEM_MAX and
+// in the output rows beyond.
+#ifndef IKDG_KNN_REG_MAX
+#define IKDG_KNN_REG_MAX 16
+#endif
+constexpr int KNN_REG_MAX = IKDG_KNN_REG_MAX;
+constexpr int KNN_SMEM_MAX = 64;
 constexpr int QBIN_BITS = 16;
 constexpr int QBIN_BINS = 1 << QBIN_BITS;
 constexpr long long QBIN_MIN_QUERIES = 2048;

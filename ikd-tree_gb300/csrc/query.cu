@@ -11,8 +11,14 @@ namespace {
 
 using search::FINF;
 
+// Threads per CTA of the per-call kNN kernel.
+#ifndef IKDG_KNN_THREADS
+#define IKDG_KNN_THREADS 128
+#endif
+constexpr int KNN_THREADS = IKDG_KNN_THREADS;
+
 template <int KMAX, int G>
-__global__ void __launch_bounds__(128) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
+__global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
                                                   long long nq, int k, float max_sq, int* __restrict__ out_id,
                                                   float* __restrict__ out_d2, float* __restrict__ out_xyz,
                                                   int* __restrict__ out_cnt, int* __restrict__ slots,
@@ -59,14 +65,55 @@ template <int KMAX>
 void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
                 float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s) {
     if (lanes >= 4)
-        knn_kernel<KMAX, 4><<<blocks_for(nq * 4, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+        knn_kernel<KMAX, 4><<<blocks_for(nq * 4, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
                                                                     out_xyz, out_cnt, slots, perm);
     else if (lanes == 2)
-        knn_kernel<KMAX, 2><<<blocks_for(nq * 2, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+        knn_kernel<KMAX, 2><<<blocks_for(nq * 2, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
                                                                     out_xyz, out_cnt, slots, perm);
     else
-        knn_kernel<KMAX, 1><<<blocks_for(nq, 128), 128, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+        knn_kernel<KMAX, 1><<<blocks_for(nq, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
                                                                 out_xyz, out_cnt, slots, perm);
+}
+
+// KNN_REG_MAX < k <= KNN_SMEM_MAX: each group's sorted candidate list lives
+// in shared memory, entry j of group g at [j * groups + g] (threads of a warp
+// touching the same entry hit different banks).  64 threads per CTA keep
+// 64 entries x 12 bytes x 64 groups within the default 48 KB.
+constexpr int KNN_SMEM_THREADS = 64;
+
+template <int G>
+__global__ void __launch_bounds__(KNN_SMEM_THREADS) knn_smem_kernel(DevTree t, const float* __restrict__ q,
+                                                                    int q_stride, long long nq, int k, float max_sq,
+                                                                    int* __restrict__ out_id,
+                                                                    float* __restrict__ out_d2,
+                                                                    float* __restrict__ out_xyz,
+                                                                    int* __restrict__ out_cnt,
+                                                                    const int* __restrict__ perm) {
+    extern __shared__ float knn_sm[];
+    constexpr int groups = KNN_SMEM_THREADS / G;
+    float* sd = knn_sm;
+    int* si = reinterpret_cast<int*>(sd + groups * k);
+    int* ss = si + groups * k;
+    const int g = threadIdx.x / G;
+    const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    search::knn_body<0, G>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, nullptr, perm,
+                           sd + g, si + g, ss + g, groups);
+}
+
+void knn_smem_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
+                     float* out_d2, float* out_xyz, int* out_cnt, const int* perm, int lanes, cudaStream_t s) {
+    const int G = lanes >= 4 ? 4 : lanes == 2 ? 2 : 1;
+    const size_t smem = (size_t)(KNN_SMEM_THREADS / G) * k * 12;
+    const unsigned grid = blocks_for(nq * G, KNN_SMEM_THREADS);
+    if (G == 4)
+        knn_smem_kernel<4><<<grid, KNN_SMEM_THREADS, smem, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                out_xyz, out_cnt, perm);
+    else if (G == 2)
+        knn_smem_kernel<2><<<grid, KNN_SMEM_THREADS, smem, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                out_xyz, out_cnt, perm);
+    else
+        knn_smem_kernel<1><<<grid, KNN_SMEM_THREADS, smem, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                out_xyz, out_cnt, perm);
 }
 
 // ---- query binning -----------------------------------------------------------
@@ -107,7 +154,7 @@ __global__ void qbin_scatter_kernel(const int* __restrict__ key, long long nq, i
 size_t knn_temp_bytes(long long nq, int k) {
     size_t b = 0;
     if (nq >= QBIN_MIN_QUERIES) b += sizeof(int) * (2 * QBIN_BINS + 2 * nq) + scan_temp_bytes(QBIN_BINS) + 1024;
-    if (k > KNN_REG_MAX) b += sizeof(int) * nq * k + 256;
+    if (k > KNN_SMEM_MAX) b += sizeof(int) * nq * k + 256;
     return b;
 }
 
@@ -131,11 +178,13 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
         qbin_scatter_kernel<<<blocks_for(nq, 256), 256, 0, s>>>(key, nq, offs, pm);
         perm = pm;
     }
-    int* slots = k > KNN_REG_MAX ? (int*)tp : nullptr;
+    int* slots = k > KNN_SMEM_MAX ? (int*)tp : nullptr;
 #define IKDG_KNN(KM) \
     knn_launch<KM>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm, lanes, s)
-    if (k > KNN_REG_MAX)
+    if (k > KNN_SMEM_MAX)
         IKDG_KNN(0);
+    else if (k > KNN_REG_MAX)
+        knn_smem_launch(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, perm, lanes, s);
     else if (k <= 1)
         IKDG_KNN(1);
     else if (k <= 2)
@@ -148,10 +197,8 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
         IKDG_KNN(8);
     else if (k <= 16)
         IKDG_KNN(16);
-    else if (k <= 32)
+    else if constexpr (KNN_REG_MAX >= 32)
         IKDG_KNN(32);
-    else
-        IKDG_KNN(64);
 #undef IKDG_KNN
 }
 

@@ -22,16 +22,31 @@ namespace search {
 
 constexpr float FINF = __builtin_huge_valf();
 // Leaf slots loaded ahead of use by a one-lane kNN group.
-constexpr int LEAF_ILP = 4;
+#ifndef IKDG_LEAF_ILP
+#define IKDG_LEAF_ILP 1
+#endif
+constexpr int LEAF_ILP = IKDG_LEAF_ILP;
+// 1: the kNN traversal asks L1 for the record of a subtree it pushes and for
+// the slots of a leaf it is about to scan, ahead of use.
+#ifndef IKDG_KNN_PREFETCH
+#define IKDG_KNN_PREFETCH 0
+#endif
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+// Leaves a warp scans per step of the range search's leaf phase.
+constexpr int RANGE_LEAF_BATCH = 4;
 
 __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
     return d < d2 || (d == d2 && id < id2);
 }
 
 // KMAX > 0: the best k candidates live sorted in registers (k <= KMAX).
-// KMAX == 0: any k; the sorted candidates live in the query's output rows
-// (global memory), with the slot index parked in out_cnt-independent scratch
-// `slots` (k ints per query).
+// KMAX == 0: any k; the sorted candidates live in memory: in kd / ki / ks
+// (entry j of the list at index j * kst; shared memory in the per-call
+// kernel for k <= KNN_SMEM_MAX), or, when kd is null, in the query's output
+// rows with the slot index parked in `slots` (k ints per query).
 // Traversal of one query by a group of G consecutive lanes: nearer child
 // first, the farther one pushed with its box distance; a subtree is skipped
 // when that distance exceeds min(max_dist^2, current k-th distance).  The loop
@@ -48,7 +63,8 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                                          long long nq, int k, float max_sq, int* __restrict__ out_id,
                                          float* __restrict__ out_d2, float* __restrict__ out_xyz,
                                          int* __restrict__ out_cnt, int* __restrict__ slots,
-                                         const int* __restrict__ perm) {
+                                         const int* __restrict__ perm, float* kd = nullptr, int* ki = nullptr,
+                                         int* ks = nullptr, int kst = 1) {
     const int sub = threadIdx.x & (G - 1);
     const int lane = threadIdx.x & 31;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
@@ -68,9 +84,11 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         bi[j] = 0x7fffffff;
         bsl[j] = -1;
     }
-    float* gd = out_d2 + qi * k;
-    int* gi = out_id + qi * k;
-    int* gs = slots != nullptr ? slots + qi * k : nullptr;
+    const bool in_rows = kd == nullptr;
+    float* gd = in_rows ? out_d2 + qi * k : kd;
+    int* gi = in_rows ? out_id + qi * k : ki;
+    int* gs = in_rows ? (slots != nullptr ? slots + qi * k : nullptr) : ks;
+    const int gst = in_rows ? 1 : kst;
     int gcnt = 0;
     float worst = FINF;
     int worst_id = 0x7fffffff;
@@ -104,21 +122,21 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
             // group's first lane owns them.
             if (sub == 0) {
                 int pos = gcnt < k ? gcnt : k - 1;
-                while (pos > 0 && cand_less(d, id, gd[pos - 1], gi[pos - 1])) {
-                    gd[pos] = gd[pos - 1];
-                    gi[pos] = gi[pos - 1];
-                    gs[pos] = gs[pos - 1];
+                while (pos > 0 && cand_less(d, id, gd[(pos - 1) * gst], gi[(pos - 1) * gst])) {
+                    gd[pos * gst] = gd[(pos - 1) * gst];
+                    gi[pos * gst] = gi[(pos - 1) * gst];
+                    gs[pos * gst] = gs[(pos - 1) * gst];
                     --pos;
                 }
-                gd[pos] = d;
-                gi[pos] = id;
-                gs[pos] = sl;
+                gd[pos * gst] = d;
+                gi[pos * gst] = id;
+                gs[pos * gst] = sl;
             }
             if (gcnt < k) ++gcnt;
             if (gcnt == k) {
                 __syncwarp(gmask);
-                worst = __shfl_sync(gmask, sub == 0 ? gd[k - 1] : 0.f, lane & ~(G - 1));
-                worst_id = __shfl_sync(gmask, sub == 0 ? gi[k - 1] : 0, lane & ~(G - 1));
+                worst = __shfl_sync(gmask, sub == 0 ? gd[(k - 1) * gst] : 0.f, lane & ~(G - 1));
+                worst_id = __shfl_sync(gmask, sub == 0 ? gi[(k - 1) * gst] : 0, lane & ~(G - 1));
             }
             return;
         }
@@ -170,13 +188,17 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
             }
             if (vl && vr) {
                 const bool left_first = dl <= dr;
+                const int far = left_first ? cr : cl;
                 if (sp < MAX_STACK) {
-                    st_code[sp] = left_first ? cr : cl;
+                    st_code[sp] = far;
                     st_d[sp] = left_first ? dr : dl;
                     ++sp;
                 } else {
                     atomicOr(&t.st->err, ERR_STACK);
                 }
+                if (IKDG_KNN_PREFETCH)
+                    prefetch_l1(far > 0 ? (const void*)(t.node + 4 * far)
+                                        : (const void*)(P + (long long)code_leaf(far) * LEAF_CAP));
                 cur = left_first ? cl : cr;
             } else if (vl) {
                 cur = cl;
@@ -184,6 +206,11 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 cur = cr;
             } else {
                 pop();
+            }
+            if (IKDG_KNN_PREFETCH && !done && cur < 0) {
+                const float4* lp = P + (long long)code_leaf(cur) * LEAF_CAP;
+                prefetch_l1(lp);
+                prefetch_l1(lp + 8);
             }
         }
         // Leaf phase.
@@ -242,11 +269,9 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     if (KMAX == 0) {
         for (int j = 0; j < k; ++j) {
             const bool ok = j < gcnt;
-            const int sl = ok ? gs[j] : -1;
-            if (!ok) {
-                gi[j] = -1;
-                gd[j] = FINF;
-            }
+            const int sl = ok ? gs[j * gst] : -1;
+            out_id[qi * k + j] = ok ? gi[j * gst] : -1;
+            out_d2[qi * k + j] = ok ? gd[j * gst] : FINF;
             if (out_xyz != nullptr) {
                 float4 p = ok ? __ldg(P + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
                 out_xyz[(qi * k + j) * 3 + 0] = p.x;
@@ -382,53 +407,66 @@ __device__ __forceinline__ long long range_body(const DevTree& t, const float* _
             else
                 pop();
         }
-        // Leaf phase: every held leaf, one at a time, one lane per slot.
+        // Leaf phase: the held leaves, RANGE_LEAF_BATCH at a time, one lane per
+        // slot.  A bucket always has LEAF_CAP slots in the pool, so each slot
+        // load is issued together with the leaf's fill count.
         const bool leafwork = !done && (cur >> 1) < 0;
         unsigned lb = __ballot_sync(0xffffffffu, leafwork);
         if (lb == 0) break;
         while (lb) {
-            const int src = __ffs(lb) - 1;
-            lb &= lb - 1;
-            const int it = __shfl_sync(0xffffffffu, cur, src);
-            float h[6];
+            int src[RANGE_LEAF_BATCH];
 #pragma unroll
-            for (int a = 0; a < 6; ++a) h[a] = __shfl_sync(0xffffffffu, qa[a], src);
-            const int L = code_leaf(it >> 1);
-            const bool lcov = it & 1;
-            const int nl = min(__ldg(t.leaf_n + L), LEAF_CAP);
-            bool hit = false;
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (lane < nl) {
-                p = __ldg(P + (long long)L * LEAF_CAP + lane);
-                if (!(__float_as_uint(p.w) & F_DEL)) {
-                    if (lcov) {
+            for (int u = 0; u < RANGE_LEAF_BATCH; ++u) {
+                src[u] = lb ? __ffs(lb) - 1 : -1;
+                lb &= lb - 1;
+            }
+            float4 p[RANGE_LEAF_BATCH];
+            int nl[RANGE_LEAF_BATCH], it[RANGE_LEAF_BATCH];
+#pragma unroll
+            for (int u = 0; u < RANGE_LEAF_BATCH; ++u) {
+                if (src[u] < 0) break;
+                it[u] = __shfl_sync(0xffffffffu, cur, src[u]);
+                const int L = code_leaf(it[u] >> 1);
+                p[u] = __ldg(P + (long long)L * LEAF_CAP + lane);
+                nl[u] = __ldg(t.leaf_n + L);
+            }
+#pragma unroll
+            for (int u = 0; u < RANGE_LEAF_BATCH; ++u) {
+                if (src[u] < 0) break;
+                float h[6];
+#pragma unroll
+                for (int a = 0; a < 6; ++a) h[a] = __shfl_sync(0xffffffffu, qa[a], src[u]);
+                bool hit = false;
+                if (lane < nl[u] && !(__float_as_uint(p[u].w) & F_DEL)) {
+                    if (it[u] & 1) {
                         hit = true;
                     } else if (MODE == 0) {
-                        hit = p.x >= h[0] && p.x < h[3] && p.y >= h[1] && p.y < h[4] && p.z >= h[2] && p.z < h[5];
+                        hit = p[u].x >= h[0] && p[u].x < h[3] && p[u].y >= h[1] && p[u].y < h[4] &&
+                              p[u].z >= h[2] && p[u].z < h[5];
                     } else {
-                        hit = sq_dist(p.x, p.y, p.z, h[0], h[1], h[2]) <= h[3];
+                        hit = sq_dist(p[u].x, p[u].y, p[u].z, h[0], h[1], h[2]) <= h[3];
                     }
                 }
-            }
-            const unsigned hb = __ballot_sync(0xffffffffu, hit);
-            if (WRITE) {
-                const long long base = __shfl_sync(0xffffffffu, o + count, src);
-                const long long lim = __shfl_sync(0xffffffffu, o_lim, src);
-                if (hit) {
-                    const long long pos = base + __popc(hb & lt);
-                    if (pos < lim) {
-                        ids[pos] = (int)(__float_as_uint(p.w) & ID_MASK);
-                        if (xyz != nullptr) {
-                            xyz[pos * 3 + 0] = p.x;
-                            xyz[pos * 3 + 1] = p.y;
-                            xyz[pos * 3 + 2] = p.z;
+                const unsigned hb = __ballot_sync(0xffffffffu, hit);
+                if (WRITE) {
+                    const long long base = __shfl_sync(0xffffffffu, o + count, src[u]);
+                    const long long lim = __shfl_sync(0xffffffffu, o_lim, src[u]);
+                    if (hit) {
+                        const long long pos = base + __popc(hb & lt);
+                        if (pos < lim) {
+                            ids[pos] = (int)(__float_as_uint(p[u].w) & ID_MASK);
+                            if (xyz != nullptr) {
+                                xyz[pos * 3 + 0] = p[u].x;
+                                xyz[pos * 3 + 1] = p[u].y;
+                                xyz[pos * 3 + 2] = p[u].z;
+                            }
+                        } else {
+                            atomicOr(&t.st->err, ERR_OUTPUT);
                         }
-                    } else {
-                        atomicOr(&t.st->err, ERR_OUTPUT);
                     }
                 }
+                if (lane == src[u]) count += __popc(hb);
             }
-            if (lane == src) count += __popc(hb);
         }
         if (leafwork) pop();
     }

@@ -44,6 +44,27 @@ def assert_ranges(tree, ref, boxes, centres, radii):
         assert np.array_equal(np.sort(ids[offs[i]:offs[i + 1]]), want)
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_knn_every_list_storage(ikdg_mod, lanes):
+    """k in registers (<= 16), in shared memory (17..64) and in the output
+    rows (> 64), with 1, 2 and 4 lanes per query, with and without max_dist,
+    plus the returned points and counts."""
+    rng = np.random.default_rng(90 + lanes)
+    pts = rng.uniform(-10, 10, (20000, 3)).astype(np.float32)
+    pts[::97] = pts[1::97][: len(pts[::97])]  # exact duplicates: ties by id
+    tree, ref = ikdg_mod.KDTree(), spec.SpecTree()
+    tree.Build(pts)
+    ref.Build(pts)
+    tree.set_knn_lanes(lanes)
+    q = rng.uniform(-11, 11, (700, 3)).astype(np.float32)
+    for k in (3, 16, 17, 32, 48, 64, 65, 130):
+        for md in (np.inf, 1.3):
+            assert_knn(tree, ref, q, k, md)
+            ids, d2, xyz, cnt = tree.knn(q, k, md)
+            ok = ids >= 0
+            assert np.array_equal(xyz[ok].view(np.uint32), pts[ids[ok]].view(np.uint32))
+
+
 def random_boxes(rng, n, lo, hi, smin, smax):
     c = rng.uniform(lo, hi, (n, 3))
     s = rng.uniform(smin, smax, (n, 3))
