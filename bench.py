@@ -414,8 +414,15 @@ def cpu_baseline(pts, queries, steps: int):
         t0 = time.perf_counter()
         t.knn(queries[s % len(queries)], K, nthreads=cores)
         times.append(time.perf_counter() - t0)
-    t.close()
     qps = N_Q / statistics.median(times)
+    # one thread, on a 20k-query slice of the same batches
+    t1 = []
+    for s in range(steps):
+        t0 = time.perf_counter()
+        t.knn(queries[s % len(queries)][:20000], K, nthreads=1)
+        t1.append(time.perf_counter() - t0)
+    qps_1 = 20000 / statistics.median(t1)
+    t.close()
     # LiDAR mapping stream: kNN over all cores, mutations on one caller (the
     # reference's mutations are single-caller).
     base, scans = lidar_workload()
@@ -423,7 +430,7 @@ def cpu_baseline(pts, queries, steps: int):
     t.Build(base)
     upd = run_scans(t, scans, lambda p: t.knn(p, K, 5.0, nthreads=cores))
     t.close()
-    return {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
+    return {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port", "value_1_thread": qps_1,
             "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries; "
                       f"{LIDAR_SCANS} LiDAR scans on the {LIDAR_MAP}-point map",
             **upd}
@@ -451,6 +458,19 @@ def run_reference(args):
         "scan_knn_ms": cb["scan_knn_ms"],
     }
     print(json.dumps(line), flush=True)
+
+
+def aggregate_replicas(ms: float, e2e_ms: float, units: int, world: int):
+    """Replicas: every rank processed `units` per step; the job's step time
+    is the slowest rank's (all-reduce MAX over the default process group when
+    world > 1) and the value is the units of all ranks over that time."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms, e2e_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    return ms, e2e_ms, world * units / (ms / 1e3), world * units / (e2e_ms / 1e3)
 
 
 def run_ours(args):
@@ -547,12 +567,7 @@ def run_ours(args):
     stress = None if args.no_stress else stress_bench(ikdg, torch, local)
 
     # ---- aggregate over ranks (max time, summed throughput)
-    if world > 1:
-        t = torch.tensor([ms, e2e_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e2e_step = float(t[0]), float(t[1])
-    value = world * N_Q / (ms / 1e3)
-    e2e_value = world * N_Q / (e2e_step / 1e3)
+    ms, e2e_step, value, e2e_value = aggregate_replicas(ms, e2e_step, N_Q, world)
     peak, peak_kind = measured_peak()
     achieved = N_Q * bytes_per_query(N_MAP, K) / (ms / 1e3) / 1e9
     line = {

@@ -2,11 +2,12 @@
 // trees in one persistent launch per phase.  The reference has no batched
 // form; every request has the semantics of its per-call search (search.cuh).
 //
-// Work is cut into chunks of BATCH_THREADS threads; each CTA takes the next
-// chunk index from a device counter, finds the request it belongs to by a
-// binary search over the requests' first chunks, and runs that request's
-// search body on it.  So small requests of many trees fill the GPU together
-// and no launch is spent per request.  CTAs never wait on one another.
+// Work is cut into chunks of one warp (BATCH_CHUNK threads); each warp takes
+// the next chunk index from a device counter, finds the request it belongs to
+// by a binary search over the requests' first chunks, and runs that request's
+// search body on it.  So small requests of many trees fill the GPU together,
+// no launch is spent per request, and no warp waits for another (a warp with
+// a heavy query does not hold up the rest of its CTA).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -15,6 +16,8 @@
 
 namespace ikdg {
 namespace {
+
+constexpr int WARPS_PER_CTA = BATCH_THREADS / BATCH_CHUNK;
 
 // Last r in [lo, hi) with starts[r] <= c (starts ascending, starts[lo] <= c).
 __device__ __forceinline__ int find_req(const long long* __restrict__ starts, int lo, int hi, long long c) {
@@ -40,28 +43,27 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
                                                                      long long* __restrict__ counts,
                                                                      unsigned long long* __restrict__ ctr) {
     constexpr int KM = KC == 0 ? 1 : KC == 1 ? 2 : KC == 2 ? 4 : KC == 3 ? 8 : 16;
-    __shared__ long long s_chunk;
-    __shared__ int s_req;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        if (threadIdx.x == 0) {
-            const long long c = c_begin + (long long)atomicAdd(ctr, 1ull);
-            s_chunk = c;
-            s_req = c < c_end ? find_req(req_c1, r0, r1, c) : -1;
+        // Each warp takes its own chunk: no warp waits for another.
+        long long c = 0;
+        int r = -1;
+        if (lane == 0) {
+            c = c_begin + (long long)atomicAdd(ctr, 1ull);
+            r = c < c_end ? find_req(req_c1, r0, r1, c) : -1;
         }
-        __syncthreads();
-        const long long c = s_chunk;
-        const int r = s_req;
-        __syncthreads();  // both are rewritten by the next iteration
+        c = __shfl_sync(0xffffffffu, c, 0);
+        r = __shfl_sync(0xffffffffu, r, 0);
         if (c >= c_end) break;
         const BatchReq& R = reqs[r];
         const DevTree t = trees[R.tree];
         if constexpr (KC < BATCH_RANGE_CLASS) {
-            const long long tid = (c - R.c1) * (BATCH_THREADS / G) + threadIdx.x / G;
+            const long long tid = (c - R.c1) * (BATCH_CHUNK / G) + lane / G;
             search::knn_body<KM, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
                                     nullptr);
         } else {
             // warp-collective body: every lane calls it
-            const long long qi = (c - R.c1) * BATCH_THREADS + threadIdx.x;
+            const long long qi = (c - R.c1) * BATCH_CHUNK + lane;
             const bool valid = qi < R.nq;
             const long long n =
                 R.kind == BATCH_BOX
@@ -82,22 +84,20 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTre
                                                                     long long c_end,
                                                                     const long long* __restrict__ goff,
                                                                     unsigned long long* __restrict__ ctr) {
-    __shared__ long long s_chunk;
-    __shared__ int s_req;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        if (threadIdx.x == 0) {
-            const long long c = (long long)atomicAdd(ctr, 1ull);
-            s_chunk = c;
-            s_req = c < c_end ? __ldg(ridx + find_req(req_c2, 0, nr, c)) : -1;
+        long long c = 0;
+        int r = -1;
+        if (lane == 0) {
+            c = (long long)atomicAdd(ctr, 1ull);
+            r = c < c_end ? __ldg(ridx + find_req(req_c2, 0, nr, c)) : -1;
         }
-        __syncthreads();
-        const long long c = s_chunk;
-        const int r = s_req;
-        __syncthreads();
+        c = __shfl_sync(0xffffffffu, c, 0);
+        r = __shfl_sync(0xffffffffu, r, 0);
         if (c >= c_end) break;
         const BatchReq& R = reqs[r];
         const DevTree t = trees[R.tree];
-        const long long qi = (c - R.c2) * BATCH_THREADS + threadIdx.x;
+        const long long qi = (c - R.c2) * BATCH_CHUNK + lane;
         const long long base = goff[R.cbase];
         if (qi == 0) {
             const long long tot = goff[R.cbase + R.nq] - base;
@@ -203,15 +203,16 @@ void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long 
                          long long c_begin, long long c_end, int kclass, int lanes, long long* counts,
                          unsigned long long* ctr, int grid, cudaStream_t s) {
     if (c_end <= c_begin || r1 <= r0) return;
-    const long long chunks = c_end - c_begin;
-    const unsigned g = (unsigned)(chunks < grid ? chunks : grid);
+    const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
     search_dispatch(kclass, lanes, true, nullptr, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
 }
 
 void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
                         long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s) {
     if (c_end <= 0 || nr <= 0) return;
-    const unsigned g = (unsigned)(c_end < grid ? c_end : grid);
+    const long long ctas = (c_end + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
     batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr);
 }
 

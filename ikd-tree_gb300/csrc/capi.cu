@@ -1085,7 +1085,7 @@ struct Batch {
             const int kc = req_class(r), lanes = req_lanes(r);
             b.kclass = kc < BATCH_RANGE_CLASS ? kc : 0;
             b.lanes = lanes;
-            const long long per = kc < BATCH_RANGE_CLASS ? BATCH_THREADS / lanes : BATCH_THREADS;
+            const long long per = kc < BATCH_RANGE_CLASS ? BATCH_CHUNK / lanes : BATCH_CHUNK;
             b.c1 = chunk;
             b.n1 = (b.nq + per - 1) / per;
             chunk += b.n1;
@@ -1112,7 +1112,7 @@ struct Batch {
         for (size_t j = 0; j < range_reqs.size(); ++j) {
             BatchReq& b = d[pos_of[range_reqs[j]]];
             b.c2 = chunk2;
-            b.n2 = (b.nq + BATCH_THREADS - 1) / BATCH_THREADS;
+            b.n2 = (b.nq + BATCH_CHUNK - 1) / BATCH_CHUNK;
             if (b.n2 > 0) {
                 ridx.push_back(pos_of[range_reqs[j]]);
                 c2.push_back(chunk2);

@@ -87,9 +87,10 @@ void launch_range(const DevTree& t, int mode, const float* q, int q_stride, cons
 // One request of a multi-tree batch: a kNN, box or radius search of nq queries
 // on trees[tree].  Phase 1 (search) covers chunks [c1, c1 + n1) of the
 // phase's chunk numbering; range requests also take phase-2 (write) chunks
-// [c2, c2 + n2).  A chunk is BATCH_THREADS threads: 128 / lanes kNN queries,
-// or 128 range queries.
+// [c2, c2 + n2).  A chunk is one warp, BATCH_CHUNK threads: 32 / lanes kNN
+// queries, or 32 range queries.
 constexpr int BATCH_THREADS = 128;
+constexpr int BATCH_CHUNK = 32;
 constexpr int BATCH_KMAX = 16;
 constexpr int BATCH_RANGE_CLASS = 5;  // register class of box / radius requests
 enum BatchKind : int { BATCH_KNN = 0, BATCH_BOX = 1, BATCH_RADIUS = 2 };

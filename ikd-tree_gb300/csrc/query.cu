@@ -64,15 +64,18 @@ inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) /
 template <int KMAX>
 void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
                 float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s) {
-    if (lanes >= 4)
-        knn_kernel<KMAX, 4><<<blocks_for(nq * 4, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
-                                                                    out_xyz, out_cnt, slots, perm);
-    else if (lanes == 2)
-        knn_kernel<KMAX, 2><<<blocks_for(nq * 2, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
-                                                                    out_xyz, out_cnt, slots, perm);
+    const int G = lanes >= 4 ? 4 : lanes == 2 ? 2 : 1;
+    const unsigned grid = blocks_for(nq * G, KNN_THREADS);
+#define IKDG_KNN_G(GG)                                                                                              \
+    knn_kernel<KMAX, GG><<<grid, KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, \
+                                                      slots, perm)
+    if (G == 4)
+        IKDG_KNN_G(4);
+    else if (G == 2)
+        IKDG_KNN_G(2);
     else
-        knn_kernel<KMAX, 1><<<blocks_for(nq, KNN_THREADS), KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
-                                                                out_xyz, out_cnt, slots, perm);
+        IKDG_KNN_G(1);
+#undef IKDG_KNN_G
 }
 
 // KNN_REG_MAX < k <= KNN_SMEM_MAX: each group's sorted candidate list lives
