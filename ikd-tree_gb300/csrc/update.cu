@@ -14,8 +14,9 @@
 //     downsampling) inside the box are restored.
 //   Update / Criterion_Check / Rebuild (:1183-1323, :1089-1107, :624-645):
 //     counts and AABBs are refit bottom-up along the touched paths only; a
-//     node whose deleted share exceeds alpha_del or whose left share leaves
-//     [1 - alpha_bal, alpha_bal] is rebuilt, topmost first.
+//     node whose deleted share of slots exceeds alpha_del or whose left share
+//     of valid points leaves [1 - alpha_bal, alpha_bal] is rebuilt, topmost
+//     first.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -167,8 +168,14 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         t.nheight[X] = h;
         bool viol = false;
         if (slots > c.min_size) {
-            float fd = (float)del / (float)slots;
-            float fb = (float)cc.x / (float)slots;
+            // alpha_del on stored slots; alpha_bal on valid points.  (The
+            // reference weighs balance by sizes that still include lazily
+            // deleted nodes; here a rebuild that purges deleted points below
+            // would then unbalance the ancestors and cascade into rebuilds of
+            // ever larger subtrees, round after round.)
+            const float fd = (float)del / (float)slots;
+            const int valid = slots - del;
+            const float fb = valid > 0 ? (float)(cc.x - cc.y) / (float)valid : 0.5f;
             viol = fd > c.alpha_del || fb > c.alpha_bal || fb < 1.0f - c.alpha_bal;
         }
         // Height guard: keeps every traversal stack within MAX_STACK.
