@@ -31,10 +31,11 @@ __device__ __forceinline__ int find_req(const long long* __restrict__ starts, in
     return lo;
 }
 
-// Phase 1 for one register class: KC 0..4 are kNN requests with k <= 1, 2,
-// 4, 8, 16 (their final rows), KC = BATCH_RANGE_CLASS box and radius
-// requests (per-query hit counts in counts[cbase + qi]).  One kernel per class
-// keeps each at its own register count.
+// Phase 1 for one class: KC 0..3 are kNN requests with k <= 1, 2, 4, 8 (lists
+// in registers), KC = BATCH_SMEM_CLASS kNN with k <= 16 (lists in shared
+// memory), all producing their final rows; KC = BATCH_RANGE_CLASS box and
+// radius requests (per-query hit counts in counts[cbase + qi]).  One kernel
+// per class keeps each at its own register count.
 template <int KC, int G>
 __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTree* __restrict__ trees,
                                                                      const BatchReq* __restrict__ reqs,
@@ -42,7 +43,7 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
                                                                      int r1, long long c_begin, long long c_end,
                                                                      long long* __restrict__ counts,
                                                                      unsigned long long* __restrict__ ctr) {
-    constexpr int KM = KC == 0 ? 1 : KC == 1 ? 2 : KC == 2 ? 4 : KC == 3 ? 8 : 16;
+    constexpr int KM = KC == 0 ? 1 : KC == 1 ? 2 : KC == 2 ? 4 : 8;
     const int lane = threadIdx.x & 31;
     for (;;) {
         // Each warp takes its own chunk: no warp waits for another.
@@ -57,7 +58,19 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
         if (c >= c_end) break;
         const BatchReq& R = reqs[r];
         const DevTree t = trees[R.tree];
-        if constexpr (KC < BATCH_RANGE_CLASS) {
+        if constexpr (KC == BATCH_SMEM_CLASS) {
+            // 8 < k <= 16: each group's sorted list in shared memory, entry j
+            // of group g at [j * groups + g] (as the per-call kernel does)
+            extern __shared__ float batch_sm[];
+            constexpr int groups = BATCH_THREADS / G;
+            float* sd = batch_sm;
+            int* si = reinterpret_cast<int*>(sd + groups * BATCH_KMAX);
+            int* ss = si + groups * BATCH_KMAX;
+            const int g = threadIdx.x / G;
+            const long long tid = (c - R.c1) * (BATCH_CHUNK / G) + lane / G;
+            search::knn_body<0, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
+                                   nullptr, sd + g, si + g, ss + g, groups);
+        } else if constexpr (KC < BATCH_RANGE_CLASS) {
             const long long tid = (c - R.c1) * (BATCH_CHUNK / G) + lane / G;
             search::knn_body<KM, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
                                     nullptr);
@@ -127,13 +140,18 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTre
 
 std::mutex g_grid_mu;
 
-int resident_grid(const void* fn) {
+// Dynamic shared memory of a search kernel class (the k <= 16 lists).
+size_t class_smem(int kc, int lanes) {
+    return kc == BATCH_SMEM_CLASS ? (size_t)(BATCH_THREADS / lanes) * BATCH_KMAX * 12 : 0;
+}
+
+int resident_grid(const void* fn, size_t smem = 0) {
     // On a failed query the grid falls back to one CTA per SM (or 1); the
     // kernels are correct for any grid size.
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_THREADS, 0) != cudaSuccess) per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_THREADS, smem) != cudaSuccess) per_sm = 1;
     cudaGetLastError();
     return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
 }
@@ -148,11 +166,13 @@ template <int KC, int G>
 void search_variant(bool launch, int* grid, const DevTree* trees, const BatchReq* reqs, const long long* req_c1,
                     int r0, int r1, long long c_begin, long long c_end, long long* counts, unsigned long long* ctr,
                     unsigned g, cudaStream_t s) {
+    const size_t smem = class_smem(KC, G);
     if (!launch) {
-        *grid = resident_grid((const void*)batch_search_kernel<KC, G>);
+        *grid = resident_grid((const void*)batch_search_kernel<KC, G>, smem);
         return;
     }
-    batch_search_kernel<KC, G><<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr);
+    batch_search_kernel<KC, G><<<g, BATCH_THREADS, smem, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, counts,
+                                                              ctr);
 }
 
 template <int KC>

@@ -384,7 +384,14 @@ struct Tree {
     // Runs the jobs selected in aux (st->n_jobs on the device, nj here):
     // gather their valid points (plus overflow points), rebuild, relink and
     // refit their ancestors.
-    void run_jobs(int nj, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+    // bound: an upper bound on the jobs selected (the violator count); the
+    // job counts, totals and sizes come back in one status read.
+    void run_jobs(int bound, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
+        small.ensure(scan_temp_bytes(bound + 1) + 1024, stream);
+        launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, bound, small.p, stream);
+        read_status();
+        const int nj = st->n_jobs;
+        if (nj == 0) throw Internal{"violators without a topmost job"};
         if (debug_validate) {
             std::vector<int> jobs(nj), links(nj);
             CK(cudaMemcpyAsync(jobs.data(), aux.jobs, sizeof(int) * nj, cudaMemcpyDeviceToHost, stream));
@@ -418,9 +425,6 @@ struct Tree {
                     throw Internal{m};
                 }
         }
-        small.ensure(scan_temp_bytes(nj + 1) + 1024, stream);
-        launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, nj, small.p, stream);
-        read_status();
         long long total = st->job_total;
         long long max_job = st->max_job;
         reserve_build(total, nj);
@@ -466,11 +470,9 @@ struct Tree {
                 break;
             }
             launch_select_jobs(dt, aux, nv, stream);
-            read_status();
             dbg_round = round;
-            int nj = st->n_jobs;
-            if (nj == 0) throw Internal{"violators without a topmost job"};
-            run_jobs(nj, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
+            // at most nv jobs: run_jobs reads the job count with its own sizes
+            run_jobs(nv, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
             zero_fields(offsetof(DevStatus, n_items), sizeof(int));
             if (debug_validate) {
                 read_status();
@@ -575,7 +577,7 @@ struct Tree {
         const long long first_id = next_id;
         long long a = 0;
         while (a < n) {
-            set_status_ll(offsetof(DevStatus, count), n);
+            launch_set_ll((long long*)((char*)st_dev + offsetof(DevStatus, count)), n, stream);
             if (debug_validate) check_valid("start of a downsampling sub-batch");
             launch_ds_search(dt, n, ds_size, a, d, n_groups, stream);
             read_status();
@@ -623,10 +625,10 @@ struct Tree {
         CK(cudaMemcpyAsync(raw, boxes, sizeof(float) * m * 6, cudaMemcpyHostToDevice, stream));
         launch_delete_boxes(dt, aux, raw, m, F_DEL, (long long*)((char*)st_dev + offsetof(DevStatus, count)),
                             stream);
-        read_status();
-        long long deleted = st->count;
+        // The rebuild rounds leave `count` alone: its value arrives with the
+        // status reads of finish_update.
         finish_update(nullptr, nullptr, 0);
-        return deleted;
+        return st->count;
     }
 
     void add_boxes(const float* boxes, long long m) {

@@ -55,7 +55,7 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
 // registers for k <= KNN_REG_MAX, in shared memory for k <= KNN_SMEM_MAX and
 // in the output rows beyond.
 #ifndef IKDG_KNN_REG_MAX
-#define IKDG_KNN_REG_MAX 16
+#define IKDG_KNN_REG_MAX 8
 #endif
 constexpr int KNN_REG_MAX = IKDG_KNN_REG_MAX;
 constexpr int KNN_SMEM_MAX = 64;
@@ -92,7 +92,8 @@ void launch_range(const DevTree& t, int mode, const float* q, int q_stride, cons
 constexpr int BATCH_THREADS = 128;
 constexpr int BATCH_CHUNK = 32;
 constexpr int BATCH_KMAX = 16;
-constexpr int BATCH_RANGE_CLASS = 5;  // register class of box / radius requests
+constexpr int BATCH_SMEM_CLASS = 4;   // kNN with 8 < k <= 16: lists in shared memory
+constexpr int BATCH_RANGE_CLASS = 5;  // box / radius requests
 enum BatchKind : int { BATCH_KNN = 0, BATCH_BOX = 1, BATCH_RADIUS = 2 };
 
 struct BatchReq {

@@ -36,7 +36,10 @@ __device__ __forceinline__ void prefetch_l1(const void* p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 // Leaves a warp scans per step of the range search's leaf phase.
-constexpr int RANGE_LEAF_BATCH = 4;
+#ifndef IKDG_RANGE_LEAF_BATCH
+#define IKDG_RANGE_LEAF_BATCH 4
+#endif
+constexpr int RANGE_LEAF_BATCH = IKDG_RANGE_LEAF_BATCH;
 
 __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
     return d < d2 || (d == d2 && id < id2);

@@ -803,6 +803,8 @@ __global__ void validate_aux_leaves_kernel(DevTree t, UpdateAux a, unsigned long
     }
 }
 
+__global__ void set_ll_kernel(long long* p, long long v) { *p = v; }
+
 __global__ void snapshot_root_kernel(DevTree t) {
     int4 c = t.ncnt[0];
     t.st->root_code = __float_as_int(t.node[3].x);
@@ -1217,6 +1219,8 @@ void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts
 }
 
 void launch_snapshot_root(const DevTree& t, cudaStream_t s) { snapshot_root_kernel<<<1, 1, 0, s>>>(t); }
+
+void launch_set_ll(long long* p, long long v, cudaStream_t s) { set_ll_kernel<<<1, 1, 0, s>>>(p, v); }
 
 void launch_validate(const DevTree& t, const UpdateAux& a, bool at_rest, long long* bad, cudaStream_t s) {
     if (t.node_cap > 0)

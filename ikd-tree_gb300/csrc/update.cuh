@@ -57,6 +57,8 @@ void launch_delete_points(const DevTree& t, const UpdateAux& a, const float* pts
                           cudaStream_t s);
 void launch_add_boxes(const DevTree& t, const UpdateAux& a, const float* boxes, long long m, cudaStream_t s);
 void launch_snapshot_root(const DevTree& t, cudaStream_t s);
+// *p = v on the stream (no host wait; the value travels as a kernel argument).
+void launch_set_ll(long long* p, long long v, cudaStream_t s);
 void launch_route_append_dev_count(const DevTree& t, const UpdateAux& a, const float4* pts, long long n_bound,
                                    const int* n_dev, int4* ovf_leaf, float4* ovf_pts, cudaStream_t s);
 // Packs strided xyz input into {x, y, z, first_id + i} and flags non-finite

@@ -19,7 +19,9 @@
 //   * Add_Points on an empty tree works;
 //   * rebuilds run on the GPU synchronously, not on a background thread, so
 //     validnum() never reports -1;
-//   * flatten takes no node pointer (the tree lives in device memory).
+//   * the tree lives in device memory: Root_Node is an opaque handle that is
+//     non-null exactly while the tree stores points (code that tests it
+//     against nullptr or passes it to flatten keeps working), not a node.
 // Batched forms of the searches (Nearest_Search_Batch, Box_Search_Batch,
 // Radius_Search_Batch) run a whole set of queries in one kernel launch.
 #pragma once
@@ -64,6 +66,10 @@ class IkdgError : public std::runtime_error {
    private:
     int status_;
 };
+
+// Opaque stand-in for the reference's node type: only ever used through
+// KD_TREE::Root_Node as "is there a tree" and as flatten's first argument.
+struct KD_TREE_NODE;
 
 template <typename PointType>
 class KD_TREE {
@@ -125,6 +131,7 @@ class KD_TREE {
         std::vector<float> xyz = pack(point_cloud);
         check(ikdg_build(t_, xyz.data(), (int64_t)point_cloud.size(), 3), "Build");
         store_.assign(point_cloud.begin(), point_cloud.end());
+        refresh_root();
     }
 
     // Nearest_Search, ikd_Tree.h:236.
@@ -204,6 +211,7 @@ class KD_TREE {
               "Add_Points");
         // The device assigned ids next .. next + n - 1 to the inputs.
         store_.insert(store_.end(), PointToAdd.begin(), PointToAdd.end());
+        refresh_root();
         return (int)added;
     }
 
@@ -217,6 +225,7 @@ class KD_TREE {
     void Delete_Points(PointVector& PointToDel) {
         std::vector<float> xyz = pack(PointToDel);
         check(ikdg_delete_points(t_, xyz.data(), (int64_t)PointToDel.size(), 3), "Delete_Points");
+        refresh_root();
     }
 
     // Delete_Point_Boxes, ikd_Tree.h:242.
@@ -224,10 +233,17 @@ class KD_TREE {
         std::vector<float> b = pack_boxes(BoxPoints);
         int64_t n = 0;
         check(ikdg_delete_boxes(t_, b.data(), (int64_t)BoxPoints.size(), &n), "Delete_Point_Boxes");
+        refresh_root();
         return (int)n;
     }
 
-    // flatten(Root_Node, Storage, NOT_RECORD), ikd_Tree.h:243: the valid points.
+    // flatten(Root_Node, Storage, NOT_RECORD), ikd_Tree.h:243: the valid points
+    // (the whole tree; the node argument can only be Root_Node here).
+    void flatten(KD_TREE_NODE* root, PointVector& Storage, delete_point_storage_set storage_type) {
+        Storage.clear();
+        if (root == nullptr) return;
+        flatten(Storage, storage_type);
+    }
     void flatten(PointVector& Storage, delete_point_storage_set storage_type = NOT_RECORD) {
         (void)storage_type;
         Storage.clear();
@@ -259,14 +275,23 @@ class KD_TREE {
     }
 
     // Public members of the reference kept for source compatibility
-    // (ikd_Tree.h:246, :248); they are not used by the GPU tree.
+    // (ikd_Tree.h:246-248).  Root_Node is non-null exactly while the tree
+    // stores points (size() > 0); the others are not used by the GPU tree.
     PointVector PCL_Storage;
+    KD_TREE_NODE* Root_Node = nullptr;
     int max_queue_size = 0;
 
     ikdg_tree* handle() { return t_; }
 
    private:
+    void refresh_root() {
+        int64_t n = 0;
+        check(ikdg_size(t_, &n), "size");
+        Root_Node = n > 0 ? reinterpret_cast<KD_TREE_NODE*>(&root_token_) : nullptr;
+    }
+
     ikdg_tree* t_ = nullptr;
+    char root_token_ = 0;
     std::vector<PointType> store_;  // inserted points by id
 
     void check(int st, const char* what) {

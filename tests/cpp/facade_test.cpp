@@ -39,7 +39,9 @@ int main() {
         cloud[i].intensity = (float)i;  // payload identifies the point
     }
     Tree::Ptr tree(new Tree(0.3, 0.6, 0.2));
+    CHECK(tree->Root_Node == nullptr);  // FAST-LIO's "not built yet" test
     tree->Build(cloud);
+    CHECK(tree->Root_Node != nullptr);
     CHECK(tree->size() == 20000 && tree->validnum() == 20000);
 
     // Nearest_Search: neighbours, squared distances, payloads.
@@ -116,6 +118,9 @@ int main() {
     PV all;
     tree->flatten(all);
     CHECK((int)all.size() == tree->validnum());
+    // the reference's call shape: flatten(Root_Node, PCL_Storage, NOT_RECORD)
+    tree->flatten(tree->Root_Node, tree->PCL_Storage, NOT_RECORD);
+    CHECK(tree->PCL_Storage.size() == all.size());
     for (auto& p : all) CHECK(!(p.x >= -2 && p.x < 3 && p.y >= -2 && p.y < 3 && p.z >= -2 && p.z < 3));
     PV del(all.begin(), all.begin() + 100);
     tree->Delete_Points(del);
