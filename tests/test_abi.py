@@ -58,3 +58,30 @@ def test_status_strings(lib):
     lib.ikdg_status_string.restype = C.c_char_p
     assert lib.ikdg_status_string(0) == b"ok"
     assert lib.ikdg_status_string(3).startswith(b"output capacity")
+
+
+def test_binding_fails_loudly_without_the_library(tmp_path):
+    """No CPU fallback: without libikdg.so the binding raises instead of
+    answering from anywhere else."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "ikd-tree_gb300"))
+    import ikdg
+    saved = ikdg._lib
+    ikdg._lib = None
+    try:
+        with pytest.raises(FileNotFoundError):
+            ikdg.load(str(tmp_path / "libikdg.so"))
+    finally:
+        ikdg._lib = saved
+
+
+def test_batch_api_without_device(lib):
+    """The batch entry points are guarded like the tree ones: bad handles
+    and missing devices come back as status codes, not crashes."""
+    h = C.c_void_p()
+    st = lib.ikdg_batch_create(0, C.byref(h))
+    assert st in (0, 5, 6)  # OK, CUDA_ERR or NO_DEVICE (no GPU here)
+    if st == 0:
+        lib.ikdg_batch_destroy(h)
+    assert lib.ikdg_batch_run(None) == 2          # BAD_ARG
+    assert lib.ikdg_batch_destroy(None) == 2
