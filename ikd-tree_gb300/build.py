@@ -57,8 +57,10 @@ def build(force: bool = False) -> str:
         objs = list(ex.map(lambda s: _compile(s, force), srcs))
     if (force or not os.path.exists(LIB)
             or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs)):
+        # --no-undefined: a declaration out of step with its definition fails
+        # here instead of when the library is loaded.
         cmd = [NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs,
-               "-o", LIB, "-lcudart"]
+               "-o", LIB, "-lcudart", "-Xlinker", "--no-undefined"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
