@@ -62,6 +62,7 @@ constexpr int KNN_SMEM_MAX = 64;
 constexpr int QBIN_BITS = 16;
 constexpr int QBIN_BINS = 1 << QBIN_BITS;
 constexpr long long QBIN_MIN_QUERIES = 2048;
+constexpr long long QBIN_AUTO_QUERIES = 262144;  // default: sort batches from this size
 size_t knn_temp_bytes(long long nq, int k);
 // Allocation-free kNN: limit on the batch size and the device address of the
 // shared scratch array (looked up on the first call per device).

@@ -35,6 +35,18 @@ constexpr int LEAF_ILP = IKDG_LEAF_ILP;
 __device__ __forceinline__ void prefetch_l1(const void* p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
+// 1: the one-lane kNN leaf scan loads two slots per 256-bit load.
+#ifndef IKDG_KNN_V8
+#define IKDG_KNN_V8 0
+#endif
+
+// Two consecutive 16-byte slots from a 32-byte-aligned address, one load.
+__device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4& b) {
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
+
 // Leaves a warp scans per step of the range search's leaf phase.
 #ifndef IKDG_RANGE_LEAF_BATCH
 #define IKDG_RANGE_LEAF_BATCH 4
@@ -223,7 +235,20 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         const int L = code_leaf(cur);
         const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
         const float4* lp = P + (long long)L * LEAF_CAP;
-        if (G == 1) {
+        if (G == 1 && IKDG_KNN_V8) {
+            // Two slots per 256-bit load (slot pairs are 32-byte aligned; a
+            // bucket always has LEAF_CAP slots, so the pair never leaves it).
+            for (int j0 = 0; j0 < n; j0 += 2) {
+                float4 a, b;
+                ld_slot_pair(lp + j0, a, b);
+                const uint32_t wa = __float_as_uint(a.w);
+                if (!(wa & F_DEL))
+                    offer(sq_dist(qx, qy, qz, a.x, a.y, a.z), (int)(wa & ID_MASK), L * LEAF_CAP + j0);
+                const uint32_t wb = __float_as_uint(b.w);
+                if (j0 + 1 < n && !(wb & F_DEL))
+                    offer(sq_dist(qx, qy, qz, b.x, b.y, b.z), (int)(wb & ID_MASK), L * LEAF_CAP + j0 + 1);
+            }
+        } else if (G == 1) {
             // LEAF_ILP slot loads in flight before their candidates are
             // offered (in slot order, so the result is unchanged).
             for (int j0 = 0; j0 < n; j0 += LEAF_ILP) {

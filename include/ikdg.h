@@ -64,8 +64,9 @@ int ikdg_set_downsample_param(ikdg_tree* t, float box_length);
 /* Tuning knobs (no counterpart in the reference): points per leaf bucket
  * written by (re)builds, 8..32 (default 16); threads cooperating on one kNN
  * query, 1, 2 or 4 (default 1); tree levels used to sort a kNN batch into
- * spatially coherent order before the search, 0..16 (default 16; batches
- * under 2048 queries are never sorted). */
+ * spatially coherent order before the search: -1 (default) sorts by 16
+ * levels from 262,144 queries up and not below, 0 never sorts, 1..16 sorts
+ * every batch of at least 2048 queries. */
 int ikdg_set_leaf_fill(ikdg_tree* t, int fill);
 int ikdg_set_knn_lanes(ikdg_tree* t, int lanes);
 int ikdg_set_knn_bin_bits(ikdg_tree* t, int bits);
