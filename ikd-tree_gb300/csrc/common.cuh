@@ -174,12 +174,18 @@ struct NodeRec {
     }
 };
 
+// Read-only node record: two 256-bit loads (records are 64-byte aligned).
 __device__ __forceinline__ NodeRec load_node(const float4* __restrict__ node, int n) {
     NodeRec r;
-    r.f0 = __ldg(node + 4 * n + 0);
-    r.f1 = __ldg(node + 4 * n + 1);
-    r.f2 = __ldg(node + 4 * n + 2);
-    r.f3 = __ldg(node + 4 * n + 3);
+    const float4* p = node + 4 * n;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r.f0.x), "=f"(r.f0.y), "=f"(r.f0.z), "=f"(r.f0.w), "=f"(r.f1.x), "=f"(r.f1.y),
+                   "=f"(r.f1.z), "=f"(r.f1.w)
+                 : "l"(p));
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r.f2.x), "=f"(r.f2.y), "=f"(r.f2.z), "=f"(r.f2.w), "=f"(r.f3.x), "=f"(r.f3.y),
+                   "=f"(r.f3.z), "=f"(r.f3.w)
+                 : "l"(p + 2));
     return r;
 }
 

@@ -21,28 +21,11 @@ namespace ikdg {
 namespace search {
 
 constexpr float FINF = __builtin_huge_valf();
-// Leaf slots loaded ahead of use by a one-lane kNN group.
-#ifndef IKDG_LEAF_ILP
-#define IKDG_LEAF_ILP 1
-#endif
-constexpr int LEAF_ILP = IKDG_LEAF_ILP;
-// 1: the kNN traversal asks L1 for the record of a subtree it pushes and for
-// the slots of a leaf it is about to scan, ahead of use.
-#ifndef IKDG_KNN_PREFETCH
-#define IKDG_KNN_PREFETCH 0
-#endif
 
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-// 1: the one-lane kNN leaf scan loads two slots per 256-bit load.
-#ifndef IKDG_KNN_V8
-#define IKDG_KNN_V8 0
-#endif
-
-// Two consecutive 16-byte slots from a 32-byte-aligned address, one load.
+// Two consecutive 16-byte slots from a 32-byte-aligned address, one 256-bit
+// load (read-only data: the compiler may schedule it freely).
 __device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4& b) {
-    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
                  : "l"(p));
 }
@@ -211,9 +194,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 } else {
                     atomicOr(&t.st->err, ERR_STACK);
                 }
-                if (IKDG_KNN_PREFETCH)
-                    prefetch_l1(far > 0 ? (const void*)(t.node + 4 * far)
-                                        : (const void*)(P + (long long)code_leaf(far) * LEAF_CAP));
                 cur = left_first ? cl : cr;
             } else if (vl) {
                 cur = cl;
@@ -221,11 +201,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 cur = cr;
             } else {
                 pop();
-            }
-            if (IKDG_KNN_PREFETCH && !done && cur < 0) {
-                const float4* lp = P + (long long)code_leaf(cur) * LEAF_CAP;
-                prefetch_l1(lp);
-                prefetch_l1(lp + 8);
             }
         }
         // Leaf phase.
@@ -235,7 +210,7 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         const int L = code_leaf(cur);
         const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
         const float4* lp = P + (long long)L * LEAF_CAP;
-        if (G == 1 && IKDG_KNN_V8) {
+        if (G == 1) {
             // Two slots per 256-bit load (slot pairs are 32-byte aligned; a
             // bucket always has LEAF_CAP slots, so the pair never leaves it).
             for (int j0 = 0; j0 < n; j0 += 2) {
@@ -247,22 +222,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 const uint32_t wb = __float_as_uint(b.w);
                 if (j0 + 1 < n && !(wb & F_DEL))
                     offer(sq_dist(qx, qy, qz, b.x, b.y, b.z), (int)(wb & ID_MASK), L * LEAF_CAP + j0 + 1);
-            }
-        } else if (G == 1) {
-            // LEAF_ILP slot loads in flight before their candidates are
-            // offered (in slot order, so the result is unchanged).
-            for (int j0 = 0; j0 < n; j0 += LEAF_ILP) {
-                float4 p[LEAF_ILP];
-#pragma unroll
-                for (int u = 0; u < LEAF_ILP; ++u)
-                    p[u] = j0 + u < n ? __ldg(lp + j0 + u) : make_float4(0.f, 0.f, 0.f, __uint_as_float(F_DEL));
-#pragma unroll
-                for (int u = 0; u < LEAF_ILP; ++u) {
-                    const uint32_t w = __float_as_uint(p[u].w);
-                    if (!(w & F_DEL))
-                        offer(sq_dist(qx, qy, qz, p[u].x, p[u].y, p[u].z), (int)(w & ID_MASK),
-                              L * LEAF_CAP + j0 + u);
-                }
             }
         } else {
           for (int j0 = 0; j0 < n; j0 += G) {
