@@ -110,10 +110,36 @@ __global__ void scan_down_kernel(const T* __restrict__ in, T* __restrict__ out, 
     }
 }
 
+// One tile (n <= SCAN_TILE): the whole scan in one block, one launch.
+template <typename T>
+__global__ void scan_single_kernel(const T* __restrict__ in, T* __restrict__ out, int n, T* total) {
+    __shared__ T tile[SCAN_TILE];
+    for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) tile[i] = i < n ? in[i] : T(0);
+    __syncthreads();
+    T local[SCAN_ITEMS];
+    T sum = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        local[j] = sum;
+        sum += tile[threadIdx.x * SCAN_ITEMS + j];
+    }
+    __shared__ T tot;
+    const T ex = block_excl_scan<SCAN_THREADS>(sum, &tot);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) tile[threadIdx.x * SCAN_ITEMS + j] = local[j] + ex;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += SCAN_THREADS) out[i] = tile[i];
+    if (threadIdx.x == 0 && total != nullptr) *total = tot;
+}
+
 template <typename T>
 void exclusive_scan_t(const T* in, T* out, long long n, T* total, void* temp, cudaStream_t s) {
     if (n <= 0) {
         if (total) cudaMemsetAsync(total, 0, sizeof(T), s);
+        return;
+    }
+    if (n <= SCAN_TILE) {
+        scan_single_kernel<T><<<1, SCAN_THREADS, 0, s>>>(in, out, (int)n, total);
         return;
     }
     int tiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);

@@ -43,3 +43,29 @@ def test_lidar_stream_matches_port(ikdg_mod, port_ready):
         assert gpu.validnum() == cpu.validnum(), f"scan {s}: validnum"
         if s in (0, len(poses) - 1):
             assert G.same_point_set(gpu.flatten(), cpu.flatten()), f"scan {s}: valid point sets differ"
+
+
+def test_lidar_hundred_scans(ikdg_mod, port_ready):
+    """The whole stream of the LiDAR configuration: 100 scans.  Every scan's
+    downsampled-insert and deleted counts equal the port's, the structure
+    validates at the end, and the final valid point sets are identical; the
+    neighbours are compared on every tenth scan."""
+    world = S.lidar_world(2101)
+    base = S.lidar_map(world, 2_000_000, 2102)
+    poses = S.trajectory(100, 2103)
+    gpu = ikdg_mod.KDTree(0.5, 0.6, 0.5)
+    cpu = oracle_lib.OracleTree(0.5, 0.6, 0.5, kind="port")
+    gpu.Build(base)
+    cpu.Build(base)
+    for s, pose in enumerate(poses):
+        scan = S.lidar_scan(world, pose, 6000 + s)
+        if s % 10 == 0:
+            ids, d2, xyz, cnt = gpu.knn(scan, 5, 5.0)
+            rxyz, rd2, rcnt = cpu.knn(scan, 5, 5.0, nthreads=8)
+            G.check_knn_rows(scan, rxyz, rd2, rcnt, xyz, d2, cnt)
+        assert gpu.Add_Points(scan, True) == cpu.Add_Points(scan, True), f"scan {s}: downsampled inserts"
+        boxes = S.cube_complement_boxes((pose[0], pose[1], 1.8), 100.0)
+        assert gpu.Delete_Point_Boxes(boxes) == cpu.Delete_Point_Boxes(boxes), f"scan {s}: deleted count"
+    assert gpu.validnum() == cpu.validnum()
+    assert gpu.validate() == 0
+    assert G.same_point_set(gpu.flatten(), cpu.flatten()), "valid point sets differ after 100 scans"
