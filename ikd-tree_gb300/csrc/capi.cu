@@ -21,6 +21,7 @@
 #include "kernels.cuh"
 #include "update.cuh"
 
+
 namespace ikdg {
 namespace {
 

@@ -331,6 +331,8 @@ class KDTree:
 
     # -- streams ---------------------------------------------------------------
     def stream(self) -> int:
+        """The tree's CUDA stream (destroyed with the tree: free torch tensors
+        whose work ran on it, e.g. under torch.cuda.ExternalStream, first)."""
         s = _vp()
         self._check(self.lib.ikdg_get_stream(self.h, C.byref(s)), "get_stream")
         return s.value or 0
