@@ -15,12 +15,14 @@
 // three arrays.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "kernels.cuh"
 
 namespace ikdg {
 namespace {
 
-constexpr int LB_MAX_GLOBAL = 1024;  // = LB_MAX: segments this small go to the local builder
+constexpr int LB_MAX = 4096;  // segments this small go to the CTA-local builder
 
 constexpr int KIND_LEAF = 0;
 constexpr int KIND_NODE = 1;
@@ -80,7 +82,7 @@ __global__ void level_seg_kernel(DevTree t, const float4* __restrict__ pts, cons
     int4 sg = segs[i];
     int s = sg.x, e = sg.y, link = sg.z;
     int cnt = e - s;
-    if (cnt <= LB_MAX_GLOBAL) {
+    if (cnt <= LB_MAX) {
         int r = atomicAdd(nlocal, 1);
         if (r >= max_next) {
             atomicOr(&t.st->err, ERR_SEG);
@@ -187,10 +189,8 @@ __global__ void level_scatter_kernel(const uint32_t* __restrict__ ord, uint32_t*
     int sg = segpos[i];
     int4 info = sg >= 0 ? seginfo[sg] : make_int4(-1, 0, 0, 0);
     if (info.x != KIND_NODE) {
-        if (b == 0) {
-            segpos_next[i] = -1;
-            ord_next[i] = ord[i];  // keeps the local builder's index array whole
-        }
+        ord_next[b * n + i] = ord[b * n + i];  // keeps the local builder's three arrays whole
+        if (b == 0) segpos_next[i] = -1;
         return;
     }
     int s = segs[sg].x, mid = info.z;
@@ -204,95 +204,155 @@ __global__ void level_scatter_kernel(const uint32_t* __restrict__ ord, uint32_t*
 }
 
 // ---- CTA-local builder ----------------------------------------------------------
-// One block builds a whole subtree of up to LB_MAX points in shared memory.
-// Per level: every open segment's AABB by shared atomics on order-preserving
-// keys, the longest axis, then one bitonic sort of (segment start, coordinate
-// on the segment's axis, position) over the block's points, which sorts every
-// segment along its own axis in place; the median split is at the segment's
-// middle.  seg_of[i] names the open segment holding position i (-1 once the
-// point sits in a leaf).  With leaves of at most `fill` >= 8 points an open
-// segment holds >= 9 points, so a level never has more than
-// 2 * LB_MAX / 9 < LB_SEGS open segments.
-constexpr int LB_MAX = 1024;
-constexpr int LB_THREADS = 256;
-constexpr int LB_SEGS = 256;
+// One block builds a whole subtree of up to LB_MAX points in shared memory,
+// with the method of the global levels: three index arrays, each sorted on
+// one coordinate, are stably partitioned level by level, so every open
+// segment is the same position range in all three and its AABB is read off
+// the ends of the ranges.  Per level: one thread per open segment allocates
+// its node or leaf (the split point is the middle of the range on the split
+// axis, which already holds the left half in place); one pass over positions
+// marks each point's side and fills the leaves; a block prefix sum of the
+// left flags of the two other arrays and a scatter partition them.  Each
+// thread owns LB_PPT consecutive positions.
+//
+// The arrays arrive sorted from the global levels (`idx` != nullptr: the
+// three arrays of the level scatter, stride `stride`); jobs that never went
+// through the global levels (`idx` == nullptr: points pts[x .. y)) are sorted
+// here first, one bitonic sort per axis on (coordinate key, input position).
+//
+// With leaves of at most `fill` >= 8 points an open segment holds >= 9
+// points, so a level has at most 2 * LB_MAX / 9 < LB_SEGS open segments.
+constexpr int LB_THREADS = 1024;
+constexpr int LB_PPT = LB_MAX / LB_THREADS;
+constexpr int LB_SEGS = 1024;
+constexpr uint16_t LB_DONE = 0xffff;
+static_assert(LB_MAX % LB_THREADS == 0 && LB_MAX <= 65535, "local builder shape");
 static_assert(2 * LB_MAX / 9 < LB_SEGS, "segment table too small");
+
+struct LbShared {
+    float4 P[LB_MAX];                 // the job's points by local id (input order)
+    uint16_t ord0[3][LB_MAX];         // index arrays, one per axis (local ids)
+    union {
+        struct {
+            uint16_t ord1[3][LB_MAX];  // the other buffer of the partition
+            uint16_t seg_of[LB_MAX];   // open segment of a position, LB_DONE once in a leaf
+        } a;
+        unsigned long long K[LB_MAX];  // sort keys, only before the first level
+    } u;
+    uint32_t scanv[LB_MAX];           // exclusive prefix of packed left flags
+    uint8_t side[LB_MAX];             // per local id: 1 = goes right
+    uint16_t ss[2][LB_SEGS], se[2][LB_SEGS];
+    int slink[2][LB_SEGS];
+    int snode[LB_SEGS];               // node or leaf index, -1 when allocation failed
+    uint16_t snext[LB_SEGS];          // first child segment of a node
+    int8_t saxis[LB_SEGS];            // split axis, -1 for leaves
+    uint32_t wsum[LB_THREADS / 32];
+    int nseg[2];
+    int overflow;
+};
+static_assert(sizeof(((LbShared*)0)->u.a) == sizeof(((LbShared*)0)->u.K), "sort keys alias the second buffer");
 
 __device__ __forceinline__ float key_float(uint32_t k) {
     uint32_t u = (k & 0x80000000u) ? (k ^ 0x80000000u) : ~k;
     return __uint_as_float(u);
 }
 
+// Ascending bitonic sort of K[0 .. size), size a power of two; one
+// compare-exchange per pair, pairs spread over the block.
+__device__ void lb_bitonic(unsigned long long* K, int size) {
+    const int half = size >> 1;
+    for (int kk = 2; kk <= size; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int p = threadIdx.x; p < half; p += LB_THREADS) {
+                const int i = ((p & ~(j - 1)) << 1) | (p & (j - 1));
+                const int ixj = i | j;
+                const unsigned long long a = K[i], c = K[ixj];
+                if ((a > c) == ((i & kk) == 0)) {
+                    K[i] = c;
+                    K[ixj] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, const float4* __restrict__ pts,
                                                                  const uint32_t* __restrict__ idx,
+                                                                 long long stride, int* loc,
                                                                  const int4* __restrict__ jobs, const int* njobs,
                                                                  int fill) {
-    __shared__ float4 P[LB_MAX];
-    __shared__ unsigned long long K[LB_MAX];
-    __shared__ short seg_of[LB_MAX];
-    __shared__ int seg_s[LB_SEGS], seg_e[LB_SEGS], seg_link[LB_SEGS], seg_axis[LB_SEGS], seg_node[LB_SEGS];
-    __shared__ uint32_t bx[LB_SEGS][6];
-    __shared__ int nseg;
-    int* next_pos = reinterpret_cast<int*>(&bx[0][0]);  // reuses the dead box keys
+    extern __shared__ __align__(16) unsigned char lb_raw[];
+    LbShared& sm = *reinterpret_cast<LbShared*>(lb_raw);
     const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
     const int nj = *njobs;
     for (int job = blockIdx.x; job < nj; job += gridDim.x) {
         const int4 jb = jobs[job];
         const int n = jb.y - jb.x;
-        if (n > LB_MAX || fill < 8) {  // cannot happen: the host guarantees both
+        if (n > LB_MAX || n < 0 || fill < 8) {  // cannot happen: the host guarantees all three
             if (tid == 0) atomicOr(&t.st->err, ERR_SEG);
             continue;
         }
-        for (int i = tid; i < n; i += LB_THREADS) {
-            const long long src = idx != nullptr ? (long long)idx[jb.x + i] : (long long)jb.x + i;
-            P[i] = pts[src];
-            seg_of[i] = 0;
+        if (idx == nullptr) {
+            for (int i = tid; i < n; i += LB_THREADS) sm.P[i] = pts[(long long)jb.x + i];
+            int size = 2;
+            while (size < n) size <<= 1;
+            for (int a = 0; a < 3; ++a) {
+                __syncthreads();
+                for (int i = tid; i < size; i += LB_THREADS)
+                    sm.u.K[i] = i < n ? ((unsigned long long)float_key(coord4(sm.P[i], a)) << 32) | (unsigned)i
+                                      : ~0ull;
+                __syncthreads();
+                lb_bitonic(sm.u.K, size);
+                for (int i = tid; i < n; i += LB_THREADS) sm.ord0[a][i] = (uint16_t)sm.u.K[i];
+            }
+        } else {
+            for (int i = tid; i < n; i += LB_THREADS) {
+                const uint32_t g = idx[jb.x + i];
+                sm.P[i] = pts[g];
+                sm.ord0[0][i] = (uint16_t)i;
+                loc[g] = i;
+            }
+            __syncthreads();
+            for (int b = 1; b < 3; ++b)
+                for (int i = tid; i < n; i += LB_THREADS) sm.ord0[b][i] = (uint16_t)loc[idx[b * stride + jb.x + i]];
         }
+        __syncthreads();  // the sort keys are dead from here on
+        for (int i = tid; i < n; i += LB_THREADS) sm.u.a.seg_of[i] = 0;
         if (tid == 0) {
-            nseg = 1;
-            seg_s[0] = 0;
-            seg_e[0] = n;
-            seg_link[0] = jb.z;
+            sm.nseg[0] = 1;
+            sm.nseg[1] = 0;
+            sm.overflow = 0;
+            sm.ss[0][0] = 0;
+            sm.se[0][0] = (uint16_t)n;
+            sm.slink[0][0] = jb.z;
         }
         __syncthreads();
-        int size = 1;
-        while (size < n) size <<= 1;
+        uint16_t(*oc)[LB_MAX] = sm.ord0;
+        uint16_t(*on)[LB_MAX] = sm.u.a.ord1;
+        int cb = 0;
+        const int i0 = tid * LB_PPT;
         for (int level = 0; level < 64; ++level) {
-            const int S = nseg;
-            if (tid < S) {
-                bx[tid][0] = bx[tid][1] = bx[tid][2] = 0xffffffffu;
-                bx[tid][3] = bx[tid][4] = bx[tid][5] = 0u;
-            }
-            __syncthreads();
-            for (int i = tid; i < n; i += LB_THREADS) {
-                const int sg = seg_of[i];
-                if (sg < 0) continue;
-                const float4 p = P[i];
-                atomicMin(&bx[sg][0], float_key(p.x));
-                atomicMin(&bx[sg][1], float_key(p.y));
-                atomicMin(&bx[sg][2], float_key(p.z));
-                atomicMax(&bx[sg][3], float_key(p.x));
-                atomicMax(&bx[sg][4], float_key(p.y));
-                atomicMax(&bx[sg][5], float_key(p.z));
-            }
-            __syncthreads();
-            // One thread per open segment: a leaf, or a node with its axis.
-            if (tid < S) {
-                const int sg = tid;
-                const int s = seg_s[sg], e = seg_e[sg], link = seg_link[sg];
+            const int S = sm.nseg[cb];
+            if (S == 0) break;
+            // One thread per open segment: a leaf, or a node with its axis,
+            // its split value and two child segments.
+            for (int sg = tid; sg < S; sg += LB_THREADS) {
+                const int s = sm.ss[cb][sg], e = sm.se[cb][sg], link = sm.slink[cb][sg];
                 const int cnt = e - s;
                 const int parent = link >> 1, side = link & 1;
                 Box3 b = empty_box();
                 if (cnt > 0)
                     for (int a = 0; a < 3; ++a) {
-                        b.lo[a] = key_float(bx[sg][a]);
-                        b.hi[a] = key_float(bx[sg][3 + a]);
+                        b.lo[a] = coord4(sm.P[oc[a][s]], a);
+                        b.hi[a] = coord4(sm.P[oc[a][e - 1]], a);
                     }
-                seg_axis[sg] = -1;
-                seg_node[sg] = -1;
+                sm.saxis[sg] = -1;
+                sm.snode[sg] = -1;
                 if (cnt <= fill) {
                     const int L = alloc_leaf(t);
-                    seg_node[sg] = L;
+                    sm.snode[sg] = L;
                     if (L >= 0) {
                         t.leaf_n[L] = cnt;
                         t.lparent[L] = link;
@@ -300,137 +360,157 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                         write_child_code(t.node, parent, side, leaf_code(L));
                         write_child_cnt(t.ncnt, parent, side, cnt, 0);
                     }
-                } else {
-                    const int X = alloc_node(t);
-                    seg_node[sg] = X;
-                    if (X >= 0) {
-                        float ext[3];
-                        for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
-                        int axis = 0;
-                        if (ext[1] > ext[axis]) axis = 1;
-                        if (ext[2] > ext[axis]) axis = 2;
-                        seg_axis[sg] = axis;
-                        t.nparent[X] = link;
-                        int h = 0;
-                        for (int m = cnt; m > fill; m -= m / 2) ++h;
-                        t.nheight[X] = h;
-                        write_child_box(t.node, parent, side, b);
-                        write_child_code(t.node, parent, side, X);
-                        write_child_cnt(t.ncnt, parent, side, cnt, 0);
-                    }
-                }
-            }
-            __syncthreads();
-            // Leaves take their points; open points get sort keys.
-            for (int i = tid; i < size; i += LB_THREADS) {
-                if (i >= n) {
-                    K[i] = ~0ull;
                     continue;
                 }
-                const int sg = seg_of[i];
-                uint32_t ck = 0;
-                unsigned long long seg_key = 0;
-                if (sg >= 0) {
-                    const float4 p = P[i];
-                    const int axis = seg_axis[sg];
-                    seg_key = (unsigned long long)seg_s[sg];
-                    if (axis < 0) {
-                        const int L = seg_node[sg];
-                        if (L >= 0) {
-                            float4 q = p;
-                            q.w = __uint_as_float(__float_as_uint(p.w) & ID_MASK);
-                            t.pts[(long long)L * LEAF_CAP + (i - seg_s[sg])] = q;
-                        }
-                    } else {
-                        ck = float_key(axis == 0 ? p.x : (axis == 1 ? p.y : p.z));
+                const int X = alloc_node(t);
+                if (X < 0) continue;
+                float ext[3];
+                for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
+                int axis = 0;
+                if (ext[1] > ext[axis]) axis = 1;
+                if (ext[2] > ext[axis]) axis = 2;
+                const int mid = s + cnt / 2;
+                const int r = atomicAdd(&sm.nseg[cb ^ 1], 2);
+                if (r + 1 >= LB_SEGS) {  // cannot happen by the bound above; guard anyway
+                    atomicOr(&t.st->err, ERR_SEG);
+                    sm.overflow = 1;
+                    continue;
+                }
+                sm.snode[sg] = X;
+                sm.saxis[sg] = (int8_t)axis;
+                sm.snext[sg] = (uint16_t)r;
+                t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0),
+                                                coord4(sm.P[oc[axis][mid]], axis), __int_as_float(axis));
+                t.nparent[X] = link;
+                int h = 0;
+                for (int m = cnt; m > fill; m -= m / 2) ++h;
+                t.nheight[X] = h;
+                write_child_box(t.node, parent, side, b);
+                write_child_code(t.node, parent, side, X);
+                write_child_cnt(t.ncnt, parent, side, cnt, 0);
+                sm.ss[cb ^ 1][r] = (uint16_t)s;
+                sm.se[cb ^ 1][r] = (uint16_t)mid;
+                sm.slink[cb ^ 1][r] = X * 2;
+                sm.ss[cb ^ 1][r + 1] = (uint16_t)mid;
+                sm.se[cb ^ 1][r + 1] = (uint16_t)e;
+                sm.slink[cb ^ 1][r + 1] = X * 2 + 1;
+            }
+            __syncthreads();
+            if (sm.overflow) break;
+            // Leaves take their points; node segments mark each point's side
+            // from its position in the split axis's array.
+#pragma unroll
+            for (int r = 0; r < LB_PPT; ++r) {
+                const int i = i0 + r;
+                if (i >= n) break;
+                const int sg = sm.u.a.seg_of[i];
+                if (sg == LB_DONE) continue;
+                const int ax = sm.saxis[sg];
+                const int s = sm.ss[cb][sg];
+                if (ax < 0) {
+                    const int L = sm.snode[sg];
+                    if (L >= 0) {
+                        float4 q = sm.P[oc[0][i]];
+                        q.w = __uint_as_float(__float_as_uint(q.w) & ID_MASK);
+                        t.pts[(long long)L * LEAF_CAP + (i - s)] = q;
                     }
                 } else {
-                    seg_key = (unsigned long long)i;  // done points keep their place
+                    const int mid = s + (sm.se[cb][sg] - s) / 2;
+                    sm.side[oc[ax][i]] = i >= mid ? 1 : 0;
                 }
-                K[i] = (seg_key << 43) | ((unsigned long long)ck << 11) | (unsigned long long)i;
             }
             __syncthreads();
-            // Bitonic sort of K[0 .. size).
-            for (int kk = 2; kk <= size; kk <<= 1) {
-                for (int j = kk >> 1; j > 0; j >>= 1) {
-                    for (int i = tid; i < size; i += LB_THREADS) {
-                        const int ixj = i ^ j;
-                        if (ixj > i) {
-                            const unsigned long long a = K[i], c = K[ixj];
-                            if ((a > c) == ((i & kk) == 0)) {
-                                K[i] = c;
-                                K[ixj] = a;
-                            }
+            // Packed left flags of the two arrays that are not the split
+            // axis's: (axis + 1) % 3 in the low half, (axis + 2) % 3 in the high.
+            uint32_t v[LB_PPT];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int r = 0; r < LB_PPT; ++r) {
+                const int i = i0 + r;
+                uint32_t f = 0;
+                if (i < n) {
+                    const int sg = sm.u.a.seg_of[i];
+                    if (sg != LB_DONE) {
+                        const int ax = sm.saxis[sg];
+                        if (ax >= 0) {
+                            const int b1 = ax == 2 ? 0 : ax + 1, b2 = ax == 0 ? 2 : ax - 1;
+                            f = (uint32_t)(sm.side[oc[b1][i]] ^ 1) | ((uint32_t)(sm.side[oc[b2][i]] ^ 1) << 16);
                         }
                     }
-                    __syncthreads();
                 }
+                v[r] = sum;
+                sum += f;
             }
-            // Permute the points into sorted order.
-            float4 tmp[LB_MAX / LB_THREADS];
+            uint32_t inc = sum;
 #pragma unroll
-            for (int r = 0; r < LB_MAX / LB_THREADS; ++r) {
-                const int i = tid + r * LB_THREADS;
-                if (i < n) tmp[r] = P[K[i] & 2047ull];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
             }
+            if (lane == 31) sm.wsum[warp] = inc;
             __syncthreads();
+            if (warp == 0) {
+                uint32_t w = lane < LB_THREADS / 32 ? sm.wsum[lane] : 0u;
+                uint32_t wi = w;
 #pragma unroll
-            for (int r = 0; r < LB_MAX / LB_THREADS; ++r) {
-                const int i = tid + r * LB_THREADS;
-                if (i < n) P[i] = tmp[r];
-            }
-            // Positions of the next level's open segments (two per node).
-            if (tid == 0) {
-                int acc = 0;
-                for (int sg = 0; sg < S; ++sg) {
-                    next_pos[sg] = acc;
-                    acc += (seg_axis[sg] >= 0 && seg_node[sg] >= 0) ? 2 : 0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                    if (lane >= o) wi += y;
                 }
-                next_pos[S] = acc;
+                if (lane < LB_THREADS / 32) sm.wsum[lane] = wi - w;
             }
             __syncthreads();
-            const int S2 = next_pos[S];
-            // Split: the node's split value, the children's ranges, seg_of.
-            int ns = 0, ne = 0, nmid = 0, nX = -1, npos = -1;
-            if (tid < S && seg_axis[tid] >= 0 && seg_node[tid] >= 0) {
-                ns = seg_s[tid];
-                ne = seg_e[tid];
-                nX = seg_node[tid];
-                nmid = ns + (ne - ns) / 2;
-                const int axis = seg_axis[tid];
-                const float4 pm = P[nmid];
-                t.node[4 * nX + 3] = make_float4(__int_as_float(0), __int_as_float(0),
-                                                 axis == 0 ? pm.x : (axis == 1 ? pm.y : pm.z), __int_as_float(axis));
-                npos = next_pos[tid];
-            }
-            for (int i = tid; i < n; i += LB_THREADS) {
-                const int sg = seg_of[i];
-                if (sg < 0) continue;
-                if (seg_axis[sg] < 0 || seg_node[sg] < 0) {
-                    seg_of[i] = -1;
-                } else {
-                    const int mid = seg_s[sg] + (seg_e[sg] - seg_s[sg]) / 2;
-                    seg_of[i] = (short)(next_pos[sg] + (i < mid ? 0 : 1));
+            const uint32_t tbase = sm.wsum[warp] + inc - sum;
+#pragma unroll
+            for (int r = 0; r < LB_PPT; ++r)
+                if (i0 + r < n) sm.scanv[i0 + r] = tbase + v[r];
+            __syncthreads();
+            // Scatter: the split axis's array keeps its order, the other two
+            // are partitioned stably; positions move to the child segments.
+            if (tid == 0) sm.nseg[cb] = 0;  // every thread read it at the top of the level
+#pragma unroll
+            for (int r = 0; r < LB_PPT; ++r) {
+                const int i = i0 + r;
+                if (i >= n) break;
+                const int sg = sm.u.a.seg_of[i];
+                if (sg == LB_DONE) continue;
+                const int ax = sm.saxis[sg];
+                if (ax < 0) {
+                    sm.u.a.seg_of[i] = LB_DONE;
+                    continue;
                 }
+                const int s = sm.ss[cb][sg];
+                const int mid = s + (sm.se[cb][sg] - s) / 2;
+                const int b1 = ax == 2 ? 0 : ax + 1, b2 = ax == 0 ? 2 : ax - 1;
+                const uint32_t rel = sm.scanv[i] - sm.scanv[s];
+                on[ax][i] = oc[ax][i];
+                const uint16_t j1 = oc[b1][i], j2 = oc[b2][i];
+                const int c1 = (int)(rel & 0xffffu), c2 = (int)(rel >> 16);
+                on[b1][sm.side[j1] ? mid + (i - s - c1) : s + c1] = j1;
+                on[b2][sm.side[j2] ? mid + (i - s - c2) : s + c2] = j2;
+                sm.u.a.seg_of[i] = (uint16_t)(sm.snext[sg] + (i < mid ? 0 : 1));
             }
             __syncthreads();
-            if (S2 == 0 || S2 > LB_SEGS) {
-                if (S2 > LB_SEGS && tid == 0) atomicOr(&t.st->err, ERR_SEG);
-                break;
-            }
-            if (npos >= 0) {
-                seg_s[npos] = ns;
-                seg_e[npos] = nmid;
-                seg_link[npos] = nX * 2;
-                seg_s[npos + 1] = nmid;
-                seg_e[npos + 1] = ne;
-                seg_link[npos + 1] = nX * 2 + 1;
-            }
-            if (tid == 0) nseg = S2;
-            __syncthreads();
+            uint16_t(*tmp)[LB_MAX] = oc;
+            oc = on;
+            on = tmp;
+            cb ^= 1;
         }
         __syncthreads();
     }
+}
+
+size_t lb_smem_bytes() { return sizeof(LbShared); }
+
+// The block's shared memory is above the 48 KB default: opt in once per device.
+void lb_prepare() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(local_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LbShared));
+    done.fetch_or(bit, std::memory_order_release);
 }
 
 __global__ void finish_alloc_kernel(DevStatus* st) {
@@ -506,6 +586,7 @@ void carve_build_scratch(void* base, long long n, int njobs, int fill, BuildScra
 void build_subtrees(const DevTree& t, const float4* pts, long long n, const int* job_off, const int* job_link,
                     int njobs, long long max_job, int fill, const BuildScratch& bs, cudaStream_t s) {
     if (njobs <= 0) return;
+    lb_prepare();
     const int T = 256;
     long long nn = n > 0 ? n : 1;
     long long ms = max_segs_bound(nn, njobs, fill);
@@ -513,7 +594,8 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
     if (max_job <= LB_MAX) {
         // Every job fits one block: a single launch builds them all.
         init_segs_kernel<<<blocks_for(njobs, T), T, 0, s>>>(job_off, job_link, njobs, bs.segs[0], bs.nseg);
-        local_build_kernel<<<lb_grid, LB_THREADS, 0, s>>>(t, pts, nullptr, bs.segs[0], bs.nseg, fill);
+        local_build_kernel<<<lb_grid, LB_THREADS, lb_smem_bytes(), s>>>(t, pts, nullptr, 0, nullptr, bs.segs[0],
+                                                                         bs.nseg, fill);
         finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
         return;
     }
@@ -552,9 +634,10 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
         seg_bound = nb < ms ? nb : ms;
         cur = nxt;
     }
-    // The axis-0 index array of the last level holds every local segment.
+    // The three index arrays of the last level hold every local segment.
     unsigned g = (unsigned)(ms < 4096 ? ms : 4096);
-    local_build_kernel<<<g, LB_THREADS, 0, s>>>(t, pts, bs.ord[cur], bs.local_jobs, bs.nseg + 2, fill);
+    local_build_kernel<<<g, LB_THREADS, lb_smem_bytes(), s>>>(t, pts, bs.ord[cur], n, bs.flag, bs.local_jobs,
+                                                               bs.nseg + 2, fill);
     finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
 }
 
