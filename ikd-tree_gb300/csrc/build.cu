@@ -15,6 +15,7 @@
 // three arrays.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.cuh"
@@ -204,7 +205,7 @@ __global__ void level_scatter_kernel(const uint32_t* __restrict__ ord, uint32_t*
 }
 
 // ---- CTA-local builder ----------------------------------------------------------
-// One block builds a whole subtree of up to LB_MAX points in shared memory,
+// One block builds a whole subtree of up to MAXN points in shared memory,
 // with the method of the global levels: three index arrays, each sorted on
 // one coordinate, are stably partitioned level by level, so every open
 // segment is the same position range in all three and its AABB is read off
@@ -212,64 +213,73 @@ __global__ void level_scatter_kernel(const uint32_t* __restrict__ ord, uint32_t*
 // its node or leaf (the split point is the middle of the range on the split
 // axis, which already holds the left half in place); one pass over positions
 // marks each point's side and fills the leaves; a block prefix sum of the
-// left flags of the two other arrays and a scatter partition them.  Each
-// thread owns LB_PPT consecutive positions.
+// left flags of the two other arrays and a scatter partition them.
 //
 // The arrays arrive sorted from the global levels (`idx` != nullptr: the
 // three arrays of the level scatter, stride `stride`); jobs that never went
 // through the global levels (`idx` == nullptr: points pts[x .. y)) are sorted
-// here first, one bitonic sort per axis on (coordinate key, input position).
+// here first: one bitonic network sorts the three arrays of (coordinate key,
+// input position) together.
 //
 // With leaves of at most `fill` >= 8 points an open segment holds >= 9
-// points, so a level has at most 2 * LB_MAX / 9 < LB_SEGS open segments.
-constexpr int LB_THREADS = 1024;
-constexpr int LB_PPT = LB_MAX / LB_THREADS;
-constexpr int LB_SEGS = 1024;
+// points, so a level has at most 2 * MAXN / 9 < SEGS open segments.
+//
+// Two shapes: 4,096 points on 1,024 threads (about 207 KB of shared memory,
+// one block per SM) and 1,024 points on 256 threads (about 52 KB, four per
+// SM); each thread owns four positions and one open segment at most.
+constexpr int LB_SMALL = 1024;
 constexpr uint16_t LB_DONE = 0xffff;
-static_assert(LB_MAX % LB_THREADS == 0 && LB_MAX <= 65535, "local builder shape");
-static_assert(2 * LB_MAX / 9 < LB_SEGS, "segment table too small");
 
+template <int MAXN, int THREADS>
 struct LbShared {
-    float4 P[LB_MAX];                 // the job's points by local id (input order)
-    uint16_t ord0[3][LB_MAX];         // index arrays, one per axis (local ids)
+    static constexpr int SEGS = THREADS;
+    float4 P[MAXN];            // the job's points by local id (input order)
+    uint16_t ord0[3][MAXN];    // index arrays, one per axis (local ids)
     union {
         struct {
-            uint16_t ord1[3][LB_MAX];  // the other buffer of the partition
-            uint16_t seg_of[LB_MAX];   // open segment of a position, LB_DONE once in a leaf
+            uint16_t ord1[3][MAXN];  // the other buffer of the partition
+            uint16_t seg_of[MAXN];   // open segment of a position, LB_DONE once in a leaf
+            uint32_t scanv[MAXN];    // exclusive prefix of packed left flags
+            uint8_t side[MAXN];      // per local id: 1 = goes right
         } a;
-        unsigned long long K[LB_MAX];  // sort keys, only before the first level
+        unsigned long long K[3][MAXN];  // sort keys, only before the first level
     } u;
-    uint32_t scanv[LB_MAX];           // exclusive prefix of packed left flags
-    uint8_t side[LB_MAX];             // per local id: 1 = goes right
-    uint16_t ss[2][LB_SEGS], se[2][LB_SEGS];
-    int slink[2][LB_SEGS];
-    int snode[LB_SEGS];               // node or leaf index, -1 when allocation failed
-    uint16_t snext[LB_SEGS];          // first child segment of a node
-    int8_t saxis[LB_SEGS];            // split axis, -1 for leaves
-    uint32_t wsum[LB_THREADS / 32];
+    uint16_t ss[2][SEGS], se[2][SEGS];
+    int slink[2][SEGS];
+    int snode[SEGS];           // node or leaf index, -1 when allocation failed
+    uint16_t snext[SEGS];      // first child segment of a node
+    int8_t saxis[SEGS];        // split axis, -1 for leaves
+    uint32_t wsum[THREADS / 32];
+    PoolRun run_leaf, run_node;
     int nseg[2];
     int overflow;
 };
-static_assert(sizeof(((LbShared*)0)->u.a) == sizeof(((LbShared*)0)->u.K), "sort keys alias the second buffer");
+static_assert(sizeof(LbShared<LB_MAX, 1024>) <= 227 * 1024, "local builder shared memory");
 
 __device__ __forceinline__ float key_float(uint32_t k) {
     uint32_t u = (k & 0x80000000u) ? (k ^ 0x80000000u) : ~k;
     return __uint_as_float(u);
 }
 
-// Ascending bitonic sort of K[0 .. size), size a power of two; one
-// compare-exchange per pair, pairs spread over the block.
-__device__ void lb_bitonic(unsigned long long* K, int size) {
+// Ascending bitonic sort of K[a][0 .. size) for the three arrays at once,
+// size a power of two; one compare-exchange per pair, pairs spread over the
+// block.
+template <int MAXN, int THREADS>
+__device__ void lb_bitonic3(unsigned long long (*K)[MAXN], int size) {
     const int half = size >> 1;
     for (int kk = 2; kk <= size; kk <<= 1) {
         for (int j = kk >> 1; j > 0; j >>= 1) {
-            for (int p = threadIdx.x; p < half; p += LB_THREADS) {
+            for (int p = threadIdx.x; p < half; p += THREADS) {
                 const int i = ((p & ~(j - 1)) << 1) | (p & (j - 1));
                 const int ixj = i | j;
-                const unsigned long long a = K[i], c = K[ixj];
-                if ((a > c) == ((i & kk) == 0)) {
-                    K[i] = c;
-                    K[ixj] = a;
+                const bool up = (i & kk) == 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const unsigned long long x = K[a][i], y = K[a][ixj];
+                    if ((x > y) == up) {
+                        K[a][i] = y;
+                        K[a][ixj] = x;
+                    }
                 }
             }
             __syncthreads();
@@ -277,38 +287,52 @@ __device__ void lb_bitonic(unsigned long long* K, int size) {
     }
 }
 
-__global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, const float4* __restrict__ pts,
+template <int MAXN, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_kernel(DevTree t, const float4* __restrict__ pts,
                                                                  const uint32_t* __restrict__ idx,
                                                                  long long stride, int* loc,
                                                                  const int4* __restrict__ jobs, const int* njobs,
                                                                  int fill) {
     extern __shared__ __align__(16) unsigned char lb_raw[];
-    LbShared& sm = *reinterpret_cast<LbShared*>(lb_raw);
+    constexpr int PPT = MAXN / THREADS;
+    constexpr int SEGS = THREADS;
+    static_assert(MAXN % THREADS == 0 && PPT == 4 && MAXN <= 65535, "local builder shape");
+    static_assert(2 * MAXN / 9 < SEGS, "segment table too small");
+    LbShared<MAXN, THREADS>& sm = *reinterpret_cast<LbShared<MAXN, THREADS>*>(lb_raw);
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const int nj = *njobs;
     for (int job = blockIdx.x; job < nj; job += gridDim.x) {
         const int4 jb = jobs[job];
         const int n = jb.y - jb.x;
-        if (n > LB_MAX || n < 0 || fill < 8) {  // cannot happen: the host guarantees all three
+        if (n > MAXN || n < 0 || fill < 8) {  // cannot happen: the host guarantees all three
             if (tid == 0) atomicOr(&t.st->err, ERR_SEG);
             continue;
         }
         if (idx == nullptr) {
-            for (int i = tid; i < n; i += LB_THREADS) sm.P[i] = pts[(long long)jb.x + i];
+            for (int i = tid; i < n; i += THREADS) sm.P[i] = pts[(long long)jb.x + i];
             int size = 2;
             while (size < n) size <<= 1;
-            for (int a = 0; a < 3; ++a) {
-                __syncthreads();
-                for (int i = tid; i < size; i += LB_THREADS)
-                    sm.u.K[i] = i < n ? ((unsigned long long)float_key(coord4(sm.P[i], a)) << 32) | (unsigned)i
-                                      : ~0ull;
-                __syncthreads();
-                lb_bitonic(sm.u.K, size);
-                for (int i = tid; i < n; i += LB_THREADS) sm.ord0[a][i] = (uint16_t)sm.u.K[i];
+            __syncthreads();
+            for (int i = tid; i < size; i += THREADS) {
+                if (i < n) {
+                    const float4 p = sm.P[i];
+                    sm.u.K[0][i] = ((unsigned long long)float_key(p.x) << 32) | (unsigned)i;
+                    sm.u.K[1][i] = ((unsigned long long)float_key(p.y) << 32) | (unsigned)i;
+                    sm.u.K[2][i] = ((unsigned long long)float_key(p.z) << 32) | (unsigned)i;
+                } else {
+                    sm.u.K[0][i] = sm.u.K[1][i] = sm.u.K[2][i] = ~0ull;
+                }
+            }
+            __syncthreads();
+            lb_bitonic3<MAXN, THREADS>(sm.u.K, size);
+            for (int i = tid; i < n; i += THREADS) {
+                sm.ord0[0][i] = (uint16_t)sm.u.K[0][i];
+                sm.ord0[1][i] = (uint16_t)sm.u.K[1][i];
+                sm.ord0[2][i] = (uint16_t)sm.u.K[2][i];
             }
         } else {
-            for (int i = tid; i < n; i += LB_THREADS) {
+            for (int i = tid; i < n; i += THREADS) {
                 const uint32_t g = idx[jb.x + i];
                 sm.P[i] = pts[g];
                 sm.ord0[0][i] = (uint16_t)i;
@@ -316,10 +340,10 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
             }
             __syncthreads();
             for (int b = 1; b < 3; ++b)
-                for (int i = tid; i < n; i += LB_THREADS) sm.ord0[b][i] = (uint16_t)loc[idx[b * stride + jb.x + i]];
+                for (int i = tid; i < n; i += THREADS) sm.ord0[b][i] = (uint16_t)loc[idx[b * stride + jb.x + i]];
         }
         __syncthreads();  // the sort keys are dead from here on
-        for (int i = tid; i < n; i += LB_THREADS) sm.u.a.seg_of[i] = 0;
+        for (int i = tid; i < n; i += THREADS) sm.u.a.seg_of[i] = 0;
         if (tid == 0) {
             sm.nseg[0] = 1;
             sm.nseg[1] = 0;
@@ -329,18 +353,50 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
             sm.slink[0][0] = jb.z;
         }
         __syncthreads();
-        uint16_t(*oc)[LB_MAX] = sm.ord0;
-        uint16_t(*on)[LB_MAX] = sm.u.a.ord1;
+        uint16_t(*oc)[MAXN] = sm.ord0;
+        uint16_t(*on)[MAXN] = sm.u.a.ord1;
         int cb = 0;
-        const int i0 = tid * LB_PPT;
+        const int i0 = tid * PPT;
         for (int level = 0; level < 64; ++level) {
             const int S = sm.nseg[cb];
             if (S == 0) break;
             // One thread per open segment: a leaf, or a node with its axis,
-            // its split value and two child segments.
-            for (int sg = tid; sg < S; sg += LB_THREADS) {
-                const int s = sm.ss[cb][sg], e = sm.se[cb][sg], link = sm.slink[cb][sg];
-                const int cnt = e - s;
+            // its split value and two child segments.  The level's leaves and
+            // nodes are ranked by ballots and taken from the pools with one
+            // reservation each.
+            const int sg = tid;
+            const bool live = sg < S;
+            int s = 0, e = 0, link = 0;
+            if (live) {
+                s = sm.ss[cb][sg];
+                e = sm.se[cb][sg];
+                link = sm.slink[cb][sg];
+            }
+            const int cnt = e - s;
+            const bool is_leaf = live && cnt <= fill, is_node = live && cnt > fill;
+            const unsigned lm = __ballot_sync(0xffffffffu, is_leaf), nm = __ballot_sync(0xffffffffu, is_node);
+            if (lane == 0) sm.wsum[warp] = (uint32_t)__popc(lm) | ((uint32_t)__popc(nm) << 16);
+            __syncthreads();
+            if (warp == 0) {
+                const uint32_t w = lane < THREADS / 32 ? sm.wsum[lane] : 0u;
+                uint32_t wi = w;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                    if (lane >= o) wi += y;
+                }
+                if (lane < THREADS / 32) sm.wsum[lane] = wi - w;
+                if (lane == 31) {
+                    sm.run_leaf = pool_reserve(&t.st->free_leaf_taken, t.st->free_leaf_n, &t.st->leaf_top,
+                                               (int)(wi & 0xffffu));
+                    sm.run_node = pool_reserve(&t.st->free_node_taken, t.st->free_node_n, &t.st->node_top,
+                                               (int)(wi >> 16));
+                }
+            }
+            __syncthreads();
+            if (live) {
+                const uint32_t wb = sm.wsum[warp];
+                const unsigned below = (1u << lane) - 1u;
                 const int parent = link >> 1, side = link & 1;
                 Box3 b = empty_box();
                 if (cnt > 0)
@@ -350,8 +406,9 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                     }
                 sm.saxis[sg] = -1;
                 sm.snode[sg] = -1;
-                if (cnt <= fill) {
-                    const int L = alloc_leaf(t);
+                if (is_leaf) {
+                    const int L = pool_pick(sm.run_leaf, t.free_leaf, t.st->free_leaf_n, t.leaf_cap,
+                                            (int)(wb & 0xffffu) + __popc(lm & below), t.st, ERR_POOL_LEAF);
                     sm.snode[sg] = L;
                     if (L >= 0) {
                         t.leaf_n[L] = cnt;
@@ -360,47 +417,47 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                         write_child_code(t.node, parent, side, leaf_code(L));
                         write_child_cnt(t.ncnt, parent, side, cnt, 0);
                     }
-                    continue;
+                } else {
+                    const int X = pool_pick(sm.run_node, t.free_node, t.st->free_node_n, t.node_cap,
+                                            (int)(wb >> 16) + __popc(nm & below), t.st, ERR_POOL);
+                    float ext[3];
+                    for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
+                    int axis = 0;
+                    if (ext[1] > ext[axis]) axis = 1;
+                    if (ext[2] > ext[axis]) axis = 2;
+                    const int mid = s + cnt / 2;
+                    const int r = X >= 0 ? atomicAdd(&sm.nseg[cb ^ 1], 2) : 0;
+                    if (X >= 0 && r + 1 >= SEGS) {  // cannot happen by the bound above; guard anyway
+                        atomicOr(&t.st->err, ERR_SEG);
+                        sm.overflow = 1;
+                    } else if (X >= 0) {
+                        sm.snode[sg] = X;
+                        sm.saxis[sg] = (int8_t)axis;
+                        sm.snext[sg] = (uint16_t)r;
+                        t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0),
+                                                        coord4(sm.P[oc[axis][mid]], axis), __int_as_float(axis));
+                        t.nparent[X] = link;
+                        int h = 0;
+                        for (int m = cnt; m > fill; m -= m / 2) ++h;
+                        t.nheight[X] = h;
+                        write_child_box(t.node, parent, side, b);
+                        write_child_code(t.node, parent, side, X);
+                        write_child_cnt(t.ncnt, parent, side, cnt, 0);
+                        sm.ss[cb ^ 1][r] = (uint16_t)s;
+                        sm.se[cb ^ 1][r] = (uint16_t)mid;
+                        sm.slink[cb ^ 1][r] = X * 2;
+                        sm.ss[cb ^ 1][r + 1] = (uint16_t)mid;
+                        sm.se[cb ^ 1][r + 1] = (uint16_t)e;
+                        sm.slink[cb ^ 1][r + 1] = X * 2 + 1;
+                    }
                 }
-                const int X = alloc_node(t);
-                if (X < 0) continue;
-                float ext[3];
-                for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
-                int axis = 0;
-                if (ext[1] > ext[axis]) axis = 1;
-                if (ext[2] > ext[axis]) axis = 2;
-                const int mid = s + cnt / 2;
-                const int r = atomicAdd(&sm.nseg[cb ^ 1], 2);
-                if (r + 1 >= LB_SEGS) {  // cannot happen by the bound above; guard anyway
-                    atomicOr(&t.st->err, ERR_SEG);
-                    sm.overflow = 1;
-                    continue;
-                }
-                sm.snode[sg] = X;
-                sm.saxis[sg] = (int8_t)axis;
-                sm.snext[sg] = (uint16_t)r;
-                t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0),
-                                                coord4(sm.P[oc[axis][mid]], axis), __int_as_float(axis));
-                t.nparent[X] = link;
-                int h = 0;
-                for (int m = cnt; m > fill; m -= m / 2) ++h;
-                t.nheight[X] = h;
-                write_child_box(t.node, parent, side, b);
-                write_child_code(t.node, parent, side, X);
-                write_child_cnt(t.ncnt, parent, side, cnt, 0);
-                sm.ss[cb ^ 1][r] = (uint16_t)s;
-                sm.se[cb ^ 1][r] = (uint16_t)mid;
-                sm.slink[cb ^ 1][r] = X * 2;
-                sm.ss[cb ^ 1][r + 1] = (uint16_t)mid;
-                sm.se[cb ^ 1][r + 1] = (uint16_t)e;
-                sm.slink[cb ^ 1][r + 1] = X * 2 + 1;
             }
             __syncthreads();
             if (sm.overflow) break;
             // Leaves take their points; node segments mark each point's side
             // from its position in the split axis's array.
 #pragma unroll
-            for (int r = 0; r < LB_PPT; ++r) {
+            for (int r = 0; r < PPT; ++r) {
                 const int i = i0 + r;
                 if (i >= n) break;
                 const int sg = sm.u.a.seg_of[i];
@@ -416,16 +473,16 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                     }
                 } else {
                     const int mid = s + (sm.se[cb][sg] - s) / 2;
-                    sm.side[oc[ax][i]] = i >= mid ? 1 : 0;
+                    sm.u.a.side[oc[ax][i]] = i >= mid ? 1 : 0;
                 }
             }
             __syncthreads();
             // Packed left flags of the two arrays that are not the split
             // axis's: (axis + 1) % 3 in the low half, (axis + 2) % 3 in the high.
-            uint32_t v[LB_PPT];
+            uint32_t v[PPT];
             uint32_t sum = 0;
 #pragma unroll
-            for (int r = 0; r < LB_PPT; ++r) {
+            for (int r = 0; r < PPT; ++r) {
                 const int i = i0 + r;
                 uint32_t f = 0;
                 if (i < n) {
@@ -434,7 +491,7 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                         const int ax = sm.saxis[sg];
                         if (ax >= 0) {
                             const int b1 = ax == 2 ? 0 : ax + 1, b2 = ax == 0 ? 2 : ax - 1;
-                            f = (uint32_t)(sm.side[oc[b1][i]] ^ 1) | ((uint32_t)(sm.side[oc[b2][i]] ^ 1) << 16);
+                            f = (uint32_t)(sm.u.a.side[oc[b1][i]] ^ 1) | ((uint32_t)(sm.u.a.side[oc[b2][i]] ^ 1) << 16);
                         }
                     }
                 }
@@ -450,26 +507,26 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
             if (lane == 31) sm.wsum[warp] = inc;
             __syncthreads();
             if (warp == 0) {
-                uint32_t w = lane < LB_THREADS / 32 ? sm.wsum[lane] : 0u;
+                uint32_t w = lane < THREADS / 32 ? sm.wsum[lane] : 0u;
                 uint32_t wi = w;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
                     if (lane >= o) wi += y;
                 }
-                if (lane < LB_THREADS / 32) sm.wsum[lane] = wi - w;
+                if (lane < THREADS / 32) sm.wsum[lane] = wi - w;
             }
             __syncthreads();
             const uint32_t tbase = sm.wsum[warp] + inc - sum;
 #pragma unroll
-            for (int r = 0; r < LB_PPT; ++r)
-                if (i0 + r < n) sm.scanv[i0 + r] = tbase + v[r];
+            for (int r = 0; r < PPT; ++r)
+                if (i0 + r < n) sm.u.a.scanv[i0 + r] = tbase + v[r];
             __syncthreads();
             // Scatter: the split axis's array keeps its order, the other two
             // are partitioned stably; positions move to the child segments.
             if (tid == 0) sm.nseg[cb] = 0;  // every thread read it at the top of the level
 #pragma unroll
-            for (int r = 0; r < LB_PPT; ++r) {
+            for (int r = 0; r < PPT; ++r) {
                 const int i = i0 + r;
                 if (i >= n) break;
                 const int sg = sm.u.a.seg_of[i];
@@ -482,16 +539,16 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
                 const int s = sm.ss[cb][sg];
                 const int mid = s + (sm.se[cb][sg] - s) / 2;
                 const int b1 = ax == 2 ? 0 : ax + 1, b2 = ax == 0 ? 2 : ax - 1;
-                const uint32_t rel = sm.scanv[i] - sm.scanv[s];
+                const uint32_t rel = sm.u.a.scanv[i] - sm.u.a.scanv[s];
                 on[ax][i] = oc[ax][i];
                 const uint16_t j1 = oc[b1][i], j2 = oc[b2][i];
                 const int c1 = (int)(rel & 0xffffu), c2 = (int)(rel >> 16);
-                on[b1][sm.side[j1] ? mid + (i - s - c1) : s + c1] = j1;
-                on[b2][sm.side[j2] ? mid + (i - s - c2) : s + c2] = j2;
+                on[b1][sm.u.a.side[j1] ? mid + (i - s - c1) : s + c1] = j1;
+                on[b2][sm.u.a.side[j2] ? mid + (i - s - c2) : s + c2] = j2;
                 sm.u.a.seg_of[i] = (uint16_t)(sm.snext[sg] + (i < mid ? 0 : 1));
             }
             __syncthreads();
-            uint16_t(*tmp)[LB_MAX] = oc;
+            uint16_t(*tmp)[MAXN] = oc;
             oc = on;
             on = tmp;
             cb ^= 1;
@@ -500,17 +557,307 @@ __global__ void __launch_bounds__(LB_THREADS) local_build_kernel(DevTree t, cons
     }
 }
 
-size_t lb_smem_bytes() { return sizeof(LbShared); }
+// ---- CTA-per-job splitter for medium jobs -----------------------------------------
+// Jobs of up to MID_MAX points skip the global sort: one block per job splits
+// it level by level until every open segment fits the small local builder
+// (LB_SMALL points), whole segments at a time.  Per segment: the AABB by a block reduction of
+// order-preserving keys; the median key on the longest axis by a four-pass
+// radix select (8-bit digits, shared histogram); then one stable partition
+// pass.  Keys below the median go left, keys equal to it go left in position
+// order until the left half holds n / 2 points, so the split is the same
+// (point of rank n / 2 on the axis, ties by position) as in the sorted
+// builders.  Points move between two scratch buffers (level 0 reads the
+// input); segments that fit the small local builder are copied to buffer 0
+// if they are not there and handed to it as jobs.
+constexpr int MID_MAX = 1 << 17;
+constexpr int MID_THREADS = 1024;
+constexpr int MID_PPT = 4;
+constexpr int MID_TILE = MID_THREADS * MID_PPT;
+constexpr int MID_SEGS = 2 * (MID_MAX / LB_SMALL) + 2;  // open segments hold > LB_SMALL points each
 
-// The block's shared memory is above the 48 KB default: opt in once per device.
-void lb_prepare() {
-    static std::atomic<unsigned long long> done{0};
+struct MidShared {
+    int hist[256];
+    uint32_t red[MID_THREADS / 32][6];
+    uint32_t wsum[MID_THREADS / 32];
+    uint32_t tot;
+    int4 seg[2][MID_SEGS];
+    int nseg[2];
+    uint32_t box[6];
+    int node, axis, digit, rank;
+};
+
+// Exclusive block prefix of a per-thread value; the block total goes to
+// *total.  The shared words are free for reuse when it returns.
+__device__ __forceinline__ uint32_t mid_block_scan(uint32_t v, uint32_t* wsum, uint32_t* tot, uint32_t* total) {
+    static_assert(MID_THREADS == 32 * 32, "one warp scans the warp sums");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = wsum[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        wsum[lane] = wi - w;
+        if (lane == 31) *tot = wi;
+    }
+    __syncthreads();
+    const uint32_t r = wsum[warp] + inc - v;
+    *total = *tot;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(MID_THREADS, 1) mid_split_kernel(DevTree t, const float4* pts,
+                                                                const int* __restrict__ job_off,
+                                                                const int* __restrict__ job_link, int njobs,
+                                                                float4* buf0, float4* buf1, uint32_t* keys,
+                                                                int4* __restrict__ local_jobs, int* nlocal,
+                                                                int max_local, int fill) {
+    __shared__ MidShared sm;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int job = blockIdx.x; job < njobs; job += gridDim.x) {
+        if (tid == 0) {
+            sm.seg[0][0] = make_int4(job_off[job], job_off[job + 1], job_link[job], 0);
+            sm.nseg[0] = 1;
+        }
+        __syncthreads();
+        int cur = 0;
+        for (int level = 0; level < 32; ++level) {
+            const int S = sm.nseg[cur];
+            if (S == 0) break;
+            const float4* src = level == 0 ? pts : ((level & 1) ? buf0 : buf1);
+            float4* dst = (level & 1) ? buf1 : buf0;
+            if (tid == 0) sm.nseg[cur ^ 1] = 0;
+            for (int q = 0; q < S; ++q) {
+                const int4 sg = sm.seg[cur][q];
+                const int s = sg.x, e = sg.y, link = sg.z;
+                const int cnt = e - s;
+                __syncthreads();  // sm.seg / nseg reads done before they change
+                if (cnt <= LB_SMALL) {  // only at level 0: a small job goes straight to the local builder
+                    for (int i = s + tid; i < e; i += MID_THREADS) buf0[i] = src[i];
+                    if (tid == 0) {
+                        const int r = atomicAdd(nlocal, 1);
+                        if (r < max_local) local_jobs[r] = make_int4(s, e, link, 0);
+                        else atomicOr(&t.st->err, ERR_SEG);
+                    }
+                    continue;
+                }
+                // AABB.
+                uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+                for (int i = s + tid; i < e; i += MID_THREADS) {
+                    const float4 p = src[i];
+                    const uint32_t kx = float_key(p.x), ky = float_key(p.y), kz = float_key(p.z);
+                    mn[0] = min(mn[0], kx), mx[0] = max(mx[0], kx);
+                    mn[1] = min(mn[1], ky), mx[1] = max(mx[1], ky);
+                    mn[2] = min(mn[2], kz), mx[2] = max(mx[2], kz);
+                }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    mn[a] = __reduce_min_sync(0xffffffffu, mn[a]);
+                    mx[a] = __reduce_max_sync(0xffffffffu, mx[a]);
+                }
+                if (lane == 0)
+                    for (int a = 0; a < 3; ++a) sm.red[warp][a] = mn[a], sm.red[warp][3 + a] = mx[a];
+                __syncthreads();
+                if (warp == 0) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        uint32_t lo = lane < MID_THREADS / 32 ? sm.red[lane][a] : 0xffffffffu;
+                        uint32_t hi = lane < MID_THREADS / 32 ? sm.red[lane][3 + a] : 0u;
+                        lo = __reduce_min_sync(0xffffffffu, lo);
+                        hi = __reduce_max_sync(0xffffffffu, hi);
+                        if (lane == 0) sm.box[a] = lo, sm.box[3 + a] = hi;
+                    }
+                }
+                __syncthreads();
+                // The node: axis, allocation, links into its parent.
+                if (tid == 0) {
+                    Box3 b;
+                    for (int a = 0; a < 3; ++a) {
+                        b.lo[a] = key_float(sm.box[a]);
+                        b.hi[a] = key_float(sm.box[3 + a]);
+                    }
+                    float ext[3];
+                    for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
+                    int axis = 0;
+                    if (ext[1] > ext[axis]) axis = 1;
+                    if (ext[2] > ext[axis]) axis = 2;
+                    const int X = alloc_node(t);
+                    sm.node = X;
+                    sm.axis = axis;
+                    if (X >= 0) {
+                        const int parent = link >> 1, side = link & 1;
+                        t.nparent[X] = link;
+                        int h = 0;
+                        for (int m = cnt; m > fill; m -= m / 2) ++h;
+                        t.nheight[X] = h;
+                        write_child_box(t.node, parent, side, b);
+                        write_child_code(t.node, parent, side, X);
+                        write_child_cnt(t.ncnt, parent, side, cnt, 0);
+                    }
+                }
+                __syncthreads();
+                const int X = sm.node, axis = sm.axis;
+                if (X < 0) continue;  // the pool is exhausted (flagged by alloc_node): the points are dropped
+                // Radix select of the key of rank m = cnt / 2.
+                const int m = cnt / 2;
+                uint32_t prefix = 0, pmask = 0;
+                int rank = m;
+                for (int pass = 0; pass < 4; ++pass) {
+                    const int shift = 24 - 8 * pass;
+                    if (tid < 256) sm.hist[tid] = 0;
+                    __syncthreads();
+                    for (int base = s; base < e; base += MID_THREADS) {
+                        const int i = base + tid;
+                        bool ok = false;
+                        uint32_t k = 0;
+                        if (i < e) {
+                            if (pass == 0) {
+                                k = float_key(coord4(src[i], axis));
+                                keys[i] = k;
+                            } else {
+                                k = keys[i];
+                            }
+                            ok = (k & pmask) == prefix;
+                        }
+                        const int d = ok ? (int)((k >> shift) & 255u) : 256 + lane;
+                        const unsigned peers = __match_any_sync(0xffffffffu, d);
+                        if (ok && lane == __ffs(peers) - 1) atomicAdd(&sm.hist[d], __popc(peers));
+                    }
+                    __syncthreads();
+                    if (warp == 0) {
+                        int c[8], sum = 0;
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) c[j] = sm.hist[lane * 8 + j], sum += c[j];
+                        int inc = sum;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                            if (lane >= o) inc += y;
+                        }
+                        const int before = inc - sum;
+                        if (rank >= before && rank < inc) {  // exactly one lane
+                            int r = rank - before, d = lane * 8;
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                if (r < c[j]) {
+                                    d = lane * 8 + j;
+                                    break;
+                                }
+                                r -= c[j];
+                            }
+                            sm.digit = d;
+                            sm.rank = r;
+                        }
+                    }
+                    __syncthreads();
+                    prefix |= (uint32_t)sm.digit << shift;
+                    pmask |= 255u << shift;
+                    rank = sm.rank;
+                }
+                const uint32_t v = prefix;
+                const uint32_t need = (uint32_t)rank;  // keys equal to v that go left
+                if (tid == 0)
+                    t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0), key_float(v),
+                                                    __int_as_float(axis));
+                // Stable partition: left = keys below v, then the first `need`
+                // keys equal to v.  Packed counts: below v low, equal high.
+                uint32_t carry_lt = 0, carry_eq = 0;
+                for (int base = s; base < e; base += MID_TILE) {
+                    const int i0 = base + tid * MID_PPT;
+                    uint32_t kk[MID_PPT];
+                    uint32_t sum = 0;
+#pragma unroll
+                    for (int r = 0; r < MID_PPT; ++r) {
+                        const int i = i0 + r;
+                        kk[r] = i < e ? keys[i] : 0xffffffffu;
+                        if (i < e) sum += kk[r] < v ? 1u : (kk[r] == v ? 0x10000u : 0u);
+                    }
+                    uint32_t total;
+                    const uint32_t ex = mid_block_scan(sum, sm.wsum, &sm.tot, &total);
+                    uint32_t lt = carry_lt + (ex & 0xffffu), eq = carry_eq + (ex >> 16);
+#pragma unroll
+                    for (int r = 0; r < MID_PPT; ++r) {
+                        const int i = i0 + r;
+                        if (i >= e) break;
+                        const uint32_t k = kk[r];
+                        const bool left = k < v || (k == v && eq < need);
+                        const uint32_t lb = lt + (eq < need ? eq : need);
+                        const int dest = left ? s + (int)lb : s + m + (i - s - (int)lb);
+                        if (dest >= s && dest < e) dst[dest] = src[i];
+                        else atomicOr(&t.st->err, ERR_SEG);  // cannot happen: the select found rank m
+                        if (k < v) ++lt;
+                        else if (k == v) ++eq;
+                    }
+                    carry_lt += total & 0xffffu;
+                    carry_eq += total >> 16;
+                }
+                __syncthreads();  // the partition is complete before the children are read
+                // Children: small ones go to the local builder (from buffer 0),
+                // the others stay open.
+#pragma unroll 1
+                for (int c = 0; c < 2; ++c) {
+                    const int cs = c == 0 ? s : s + m, ce = c == 0 ? s + m : e;
+                    if (ce - cs <= LB_SMALL) {
+                        if (dst != buf0)
+                            for (int i = cs + tid; i < ce; i += MID_THREADS) buf0[i] = dst[i];
+                        if (tid == 0) {
+                            const int r = atomicAdd(nlocal, 1);
+                            if (r < max_local) local_jobs[r] = make_int4(cs, ce, X * 2 + c, 0);
+                            else atomicOr(&t.st->err, ERR_SEG);
+                        }
+                    } else if (tid == 0) {
+                        const int r = sm.nseg[cur ^ 1]++;
+                        if (r < MID_SEGS) sm.seg[cur ^ 1][r] = make_int4(cs, ce, X * 2 + c, 0);
+                        else atomicOr(&t.st->err, ERR_SEG);
+                    }
+                }
+            }
+            __syncthreads();
+            if (tid == 0 && sm.nseg[cur ^ 1] > MID_SEGS) sm.nseg[cur ^ 1] = MID_SEGS;
+            __syncthreads();
+            cur ^= 1;
+        }
+        __syncthreads();
+    }
+}
+
+template <int MAXN, int THREADS>
+void launch_local(unsigned grid, const DevTree& t, const float4* pts, const uint32_t* idx, long long stride, int* loc,
+                  const int4* jobs, const int* njobs, int fill, cudaStream_t s) {
+    local_build_kernel<MAXN, THREADS><<<grid, THREADS, sizeof(LbShared<MAXN, THREADS>), s>>>(t, pts, idx, stride, loc,
+                                                                                          jobs, njobs, fill);
+}
+
+// The local builders' shared memory is above the 48 KB default: opt in once
+// per device.  Returns the device's SM count: the block-per-job kernels run
+// one block per SM at most, each looping over jobs (idle blocks of 1,024
+// threads and 200 KB of shared memory still cost a wave each to launch).
+int lb_prepare() {
+    static std::atomic<int> sms[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    const unsigned long long bit = 1ull << (dev & 63);
-    if (done.load(std::memory_order_acquire) & bit) return;
-    cudaFuncSetAttribute(local_build_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LbShared));
-    done.fetch_or(bit, std::memory_order_release);
+    dev &= 63;
+    int n = sms[dev].load(std::memory_order_acquire);
+    if (n > 0) return n;
+    cudaFuncSetAttribute(local_build_kernel<LB_MAX, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(LbShared<LB_MAX, 1024>));
+    cudaFuncSetAttribute(local_build_kernel<LB_SMALL, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(LbShared<LB_SMALL, 256>));
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+    sms[dev].store(n, std::memory_order_release);
+    return n;
 }
 
 __global__ void finish_alloc_kernel(DevStatus* st) {
@@ -581,21 +928,37 @@ void carve_build_scratch(void* base, long long n, int njobs, int fill, BuildScra
     bs->local_jobs = (int4*)take(sizeof(int4) * ms);
     bs->nseg = (int*)take(sizeof(int) * 4);
     bs->temp = (void*)p;
+    // The splitter of medium jobs uses none of the sort arrays: its two point
+    // buffers (32 n bytes) lie over ord[0 .. 1] and keys[0 .. 1] (>= 48 n bytes).
+    bs->mid_pts[0] = (float4*)bs->ord[0];
+    bs->mid_pts[1] = (float4*)((char*)bs->ord[0] + align_up(sizeof(float4) * n));
 }
 
 void build_subtrees(const DevTree& t, const float4* pts, long long n, const int* job_off, const int* job_link,
                     int njobs, long long max_job, int fill, const BuildScratch& bs, cudaStream_t s) {
     if (njobs <= 0) return;
-    lb_prepare();
+    const long long sms = lb_prepare();
     const int T = 256;
     long long nn = n > 0 ? n : 1;
     long long ms = max_segs_bound(nn, njobs, fill);
-    const unsigned lb_grid = (unsigned)(njobs < 4096 ? njobs : 4096);
-    if (max_job <= LB_MAX) {
-        // Every job fits one block: a single launch builds them all.
+    // Block-per-job grids: the small local builder fits four blocks per SM,
+    // the splitter and the large local builder one.
+    auto grid = [&](long long jobs, long long per_sm) { return (unsigned)std::min(jobs, per_sm * sms); };
+    if (max_job <= LB_SMALL) {
+        // Every job fits the small local builder: one launch builds them all.
         init_segs_kernel<<<blocks_for(njobs, T), T, 0, s>>>(job_off, job_link, njobs, bs.segs[0], bs.nseg);
-        local_build_kernel<<<lb_grid, LB_THREADS, lb_smem_bytes(), s>>>(t, pts, nullptr, 0, nullptr, bs.segs[0],
-                                                                         bs.nseg, fill);
+        launch_local<LB_SMALL, 256>(grid(njobs, 4), t, pts, nullptr, 0, nullptr, bs.segs[0], bs.nseg, fill, s);
+        finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
+        return;
+    }
+    if (max_job <= MID_MAX) {
+        // Medium jobs: one block each splits down to the small builder's size.
+        reset_count_kernel<<<1, 1, 0, s>>>(bs.nseg + 2);
+        mid_split_kernel<<<grid(njobs, 1), MID_THREADS, 0, s>>>(t, pts, job_off, job_link, njobs, bs.mid_pts[0],
+                                                                 bs.mid_pts[1], (uint32_t*)bs.flag, bs.local_jobs,
+                                                                 bs.nseg + 2, (int)ms, fill);
+        launch_local<LB_SMALL, 256>(grid(ms, 4), t, bs.mid_pts[0], nullptr, 0, nullptr, bs.local_jobs, bs.nseg + 2,
+                                    fill, s);
         finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
         return;
     }
@@ -635,9 +998,7 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
         cur = nxt;
     }
     // The three index arrays of the last level hold every local segment.
-    unsigned g = (unsigned)(ms < 4096 ? ms : 4096);
-    local_build_kernel<<<g, LB_THREADS, lb_smem_bytes(), s>>>(t, pts, bs.ord[cur], n, bs.flag, bs.local_jobs,
-                                                               bs.nseg + 2, fill);
+    launch_local<LB_MAX, 1024>(grid(ms, 1), t, pts, bs.ord[cur], n, bs.flag, bs.local_jobs, bs.nseg + 2, fill, s);
     finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
 }
 

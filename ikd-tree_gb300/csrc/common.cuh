@@ -267,6 +267,31 @@ __device__ __forceinline__ int alloc_node(const DevTree& t) {
     }
     return n;
 }
+// Bulk form of the same allocation for `c` items at once: one reservation on
+// the shared counters (free stack first, then bump), then item j of the run
+// resolves to its index without further atomics.
+struct PoolRun {
+    int base;   // first free-stack slot taken
+    int nfree;  // items served by the free stack
+    int top;    // first bumped index
+};
+__device__ __forceinline__ PoolRun pool_reserve(int* taken, int free_n, int* top, int c) {
+    PoolRun r;
+    r.base = c > 0 ? atomicAdd(taken, c) : 0;
+    r.nfree = min(max(free_n - r.base, 0), c);
+    r.top = c - r.nfree > 0 ? atomicAdd(top, c - r.nfree) : 0;
+    return r;
+}
+__device__ __forceinline__ int pool_pick(const PoolRun& r, const int* free_list, int free_n, int cap, int j,
+                                         DevStatus* st, int err) {
+    if (j < r.nfree) return free_list[free_n - 1 - (r.base + j)];
+    const int x = r.top + (j - r.nfree);
+    if (x >= cap) {
+        atomicOr(&st->err, err);
+        return -1;
+    }
+    return x;
+}
 __device__ __forceinline__ int alloc_leaf(const DevTree& t) {
     int k = atomicAdd(&t.st->free_leaf_taken, 1);
     if (k < t.st->free_leaf_n) return t.free_leaf[t.st->free_leaf_n - 1 - k];

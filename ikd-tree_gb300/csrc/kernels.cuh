@@ -40,6 +40,7 @@ struct BuildScratch {
     int4* local_jobs;    // [max_segs]      {s, e, link} for the CTA-local builder
     int* nseg;           // [4] device counters (two levels, local jobs)
     void* temp;          // scan / sort temp
+    float4* mid_pts[2];  // 2 x [n] points of the medium-job splitter (alias ord / keys)
 };
 size_t build_scratch_bytes(long long n, int njobs, int fill);
 void carve_build_scratch(void* base, long long n, int njobs, int fill, BuildScratch* bs);
