@@ -468,11 +468,18 @@ struct Tree {
         // The dirty list is consumed: the next update starts a fresh one.
         zero_fields(offsetof(DevStatus, n_items), sizeof(int));
         // Rebuilding a subtree can unbalance its ancestors; each round moves
-        // the violations up, so a few rounds settle the tree.
+        // the violations up, so a few rounds settle the tree.  The root
+        // snapshot is taken before every status read: when the read finds no
+        // violators it is already the final status of the call.
+        bool settled = false;
         for (int round = 0; round < 8; ++round) {
+            launch_snapshot_root(dt, stream);
             read_status();
             int nv = st->n_viol;
-            if (nv == 0) break;
+            if (nv == 0) {
+                settled = true;
+                break;
+            }
             if (round == 7) {
                 // Still unsettled: clear the flags; the next call retries.
                 launch_clear_viol(dt, aux, nv, stream);
@@ -488,9 +495,11 @@ struct Tree {
                 if (st->n_viol == 0) check_valid("after a rebuild round");
             }
         }
-        zero_fields(offsetof(DevStatus, n_viol), sizeof(int));
-        launch_snapshot_root(dt, stream);
-        read_status();
+        if (!settled) {
+            zero_fields(offsetof(DevStatus, n_viol), sizeof(int));
+            launch_snapshot_root(dt, stream);
+            read_status();
+        }
         if (st->err & ERR_STACK) throw Internal{"tree deeper than the traversal stack"};
         if (debug_validate) check_valid("end of update");
         if (st->err & ERR_ID) throw CapacityFail{"point id space exhausted"};
@@ -610,7 +619,8 @@ struct Tree {
             a = e;
         }
         next_id += n;
-        read_status();
+        // Every sub-batch ended with a status read (finish_update, build_root
+        // or the read before it), so count2 is current.
         if (n_added) *n_added = st->count2;
     }
 
