@@ -6,13 +6,24 @@
 // AABB (first axis wins ties, :593-595).  Unlike the reference, internal nodes
 // hold no point: segments of at most `fill` points become leaf buckets.
 //
-// Method (all jobs of a call at once): each of the three coordinates is
-// radix-sorted once; the three sorted index arrays are then stably partitioned
-// level by level, so every segment stays a contiguous range in each array and
-// its AABB is read off the ends of the three ranges.  Per level: one thread per
-// segment allocates its node or leaf and links it into its parent; one thread
-// per position marks left / right; a prefix sum and a scatter partition the
-// three arrays.
+// All jobs of a call are built together, on one of three paths chosen by the
+// largest job:
+// * small (every job <= LB_SMALL points): one CTA per job builds the whole
+//   subtree in shared memory (local_build_kernel<LB_SMALL, 256>);
+// * medium (jobs <= MID_MAX): one CTA per job splits it down to LB_SMALL-point
+//   segments (mid_split_kernel: radix-selected median, stable partition), then
+//   the small local builder finishes them;
+// * large: each of the three coordinates is radix-sorted once; the three sorted
+//   index arrays are then stably partitioned level by level, so every segment
+//   stays a contiguous range in each array and its AABB is read off the ends of
+//   the three ranges.  Per level: one thread per segment allocates its node or
+//   leaf and links it into its parent; one thread per position marks left /
+//   right; a prefix sum and a scatter partition the three arrays.  Segments of
+//   at most LB_MAX points go, with their sorted arrays, to
+//   local_build_kernel<LB_MAX, 1024>.
+// All three cut a segment of n points at the point of rank n / 2 on its axis,
+// ties in input order (every partition is stable), so they follow one split
+// rule.
 #include <cuda_runtime.h>
 
 #include <algorithm>
