@@ -90,7 +90,7 @@ __global__ void level_seg_kernel(DevTree t, const float4* __restrict__ pts, cons
                                  int4* __restrict__ segs_next, int* nseg_next, int4* __restrict__ seginfo,
                                  int fill, int max_next, int4* __restrict__ local_jobs, int* nlocal) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *nseg_cur) return;
+    if (i >= *nseg_cur || i >= max_next) return;  // the count runs past the capacity only on overflow (flagged)
     int4 sg = segs[i];
     int s = sg.x, e = sg.y, link = sg.z;
     int cnt = e - s;
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
                                                                  const uint32_t* __restrict__ idx,
                                                                  long long stride, int* loc,
                                                                  const int4* __restrict__ jobs, const int* njobs,
-                                                                 int fill) {
+                                                                 int max_jobs, int fill) {
     extern __shared__ __align__(16) unsigned char lb_raw[];
     constexpr int PPT = MAXN / THREADS;
     constexpr int SEGS = THREADS;
@@ -312,7 +312,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
     LbShared<MAXN, THREADS>& sm = *reinterpret_cast<LbShared<MAXN, THREADS>*>(lb_raw);
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
-    const int nj = *njobs;
+    // The producers count past the capacity when it overflows (and flag it):
+    // never read beyond the job array.
+    const int nj = min(*njobs, max_jobs);
     for (int job = blockIdx.x; job < nj; job += gridDim.x) {
         const int4 jb = jobs[job];
         const int n = jb.y - jb.x;
@@ -845,9 +847,9 @@ __global__ void __launch_bounds__(MID_THREADS, 1) mid_split_kernel(DevTree t, co
 
 template <int MAXN, int THREADS>
 void launch_local(unsigned grid, const DevTree& t, const float4* pts, const uint32_t* idx, long long stride, int* loc,
-                  const int4* jobs, const int* njobs, int fill, cudaStream_t s) {
+                  const int4* jobs, const int* njobs, int max_jobs, int fill, cudaStream_t s) {
     local_build_kernel<MAXN, THREADS><<<grid, THREADS, sizeof(LbShared<MAXN, THREADS>), s>>>(t, pts, idx, stride, loc,
-                                                                                          jobs, njobs, fill);
+                                                                                          jobs, njobs, max_jobs, fill);
 }
 
 // The local builders' shared memory is above the 48 KB default: opt in once
@@ -882,9 +884,14 @@ __global__ void reset_count_kernel(int* c) { *c = 0; }
 
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// Bound on the segments of a level and on the local builders' jobs of one
+// call: a level holds at most two segments per node of the level above (each
+// node has more than `fill` points); a local job is a whole job or a piece of
+// at least 512 points (half of a segment above LB_SMALL or LB_MAX points).
 long long max_segs_bound(long long n, int njobs, int fill) {
     long long b = 2 * (n / (fill + 1)) + 2;
-    return b > njobs ? b : njobs;
+    long long j = (long long)njobs + n / 512 + 2;
+    return b > j ? b : j;
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -958,7 +965,7 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
     if (max_job <= LB_SMALL) {
         // Every job fits the small local builder: one launch builds them all.
         init_segs_kernel<<<blocks_for(njobs, T), T, 0, s>>>(job_off, job_link, njobs, bs.segs[0], bs.nseg);
-        launch_local<LB_SMALL, 256>(grid(njobs, 4), t, pts, nullptr, 0, nullptr, bs.segs[0], bs.nseg, fill, s);
+        launch_local<LB_SMALL, 256>(grid(njobs, 4), t, pts, nullptr, 0, nullptr, bs.segs[0], bs.nseg, njobs, fill, s);
         finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
         return;
     }
@@ -969,7 +976,7 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
                                                                  bs.mid_pts[1], (uint32_t*)bs.flag, bs.local_jobs,
                                                                  bs.nseg + 2, (int)ms, fill);
         launch_local<LB_SMALL, 256>(grid(ms, 4), t, bs.mid_pts[0], nullptr, 0, nullptr, bs.local_jobs, bs.nseg + 2,
-                                    fill, s);
+                                    (int)ms, fill, s);
         finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
         return;
     }
@@ -1009,7 +1016,8 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
         cur = nxt;
     }
     // The three index arrays of the last level hold every local segment.
-    launch_local<LB_MAX, 1024>(grid(ms, 1), t, pts, bs.ord[cur], n, bs.flag, bs.local_jobs, bs.nseg + 2, fill, s);
+    launch_local<LB_MAX, 1024>(grid(ms, 1), t, pts, bs.ord[cur], n, bs.flag, bs.local_jobs, bs.nseg + 2, (int)ms,
+                               fill, s);
     finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
 }
 
