@@ -93,3 +93,46 @@ def test_spec_knn_matches_port_distances(port_lib):
         ids, sd2 = s.knn(q, k, md)
         assert np.array_equal(cnt, (ids >= 0).sum(1))
         assert np.array_equal(G.bits(d2), G.bits(sd2))
+
+
+@pytest.mark.skipif(not oracle_lib.available("ref"), reason="reference not built on this machine")
+@pytest.mark.parametrize("kind", ["same", "plane", "lattice"])
+def test_oracles_match_reference_on_tied_inputs(port_lib, kind):
+    # The degenerate inputs of the GPU builder tests, small: every split key
+    # ties.  Reference, port and model agree on kNN distances, box-search
+    # sets, box-delete counts and the surviving points.
+    rng = np.random.default_rng(31 + ["same", "plane", "lattice"].index(kind))
+    n = 3000
+    if kind == "same":
+        pts = np.full((n, 3), 1.5, np.float32)
+    elif kind == "plane":
+        pts = rng.uniform(-10, 10, (n, 3)).astype(np.float32)
+        pts[:, 2] = 0.0
+    else:
+        pts = rng.integers(-4, 4, (n, 3)).astype(np.float32)
+    T = {k: oracle_lib.OracleTree(0.5, 0.6, 0.2, kind=k) for k in ("ref", "port")}
+    s = spec.SpecTree()
+    for t in T.values():
+        t.Build(pts)
+    s.Build(pts)
+    q = (pts[rng.choice(n, 100)] + rng.normal(0, 0.7, (100, 3))).astype(np.float32)
+    for k in (1, 5, 16):
+        d2 = {name: t.knn(q, k)[1] for name, t in T.items()}
+        _, sd2 = s.knn(q, k)
+        assert np.array_equal(G.bits(d2["ref"]), G.bits(d2["port"]))
+        assert np.array_equal(G.bits(d2["ref"]), G.bits(sd2))
+    c = pts[rng.choice(n, 5)]
+    h = rng.uniform(0.5, 3, (5, 3)).astype(np.float32)
+    bx = np.concatenate([c - h, c + h], 1).astype(np.float32)
+    (ro, rx), (po, px) = T["ref"].box_search(bx), T["port"].box_search(bx)
+    want = s.box_search(bx)
+    for i in range(len(bx)):
+        assert G.same_point_set(rx[ro[i]:ro[i + 1]], px[po[i]:po[i + 1]])
+        assert ro[i + 1] - ro[i] == len(want[i])
+    nd = {name: t.Delete_Point_Boxes(bx[:2]) for name, t in T.items()}
+    assert nd["ref"] == nd["port"] == s.Delete_Point_Boxes(bx[:2])
+    assert T["ref"].validnum() == T["port"].validnum() == s.validnum()
+    assert G.same_point_set(T["ref"].flatten(), T["port"].flatten())
+    assert G.same_point_set(T["ref"].flatten(), s.valid_points()[0])
+    for t in T.values():
+        t.close()
