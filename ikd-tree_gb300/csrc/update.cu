@@ -147,6 +147,10 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             atomicOr(&t.st->err, ERR_LOOP);
             return;
         }
+        // X's child codes do not change during a refit: read before arriving,
+        // they let the last walker load the children's heights together with
+        // the record instead of after it.
+        const float2 kids = __ldcg(reinterpret_cast<const float2*>(t.node + 4 * X + 3));
         // pend[X] is read before arriving: it cannot change until every
         // walker has arrived (the last one resets it), whereas after the
         // arrival the last walker may already have reset it to 0.
@@ -157,6 +161,7 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         __threadfence();  // acquire: the other children's writes are visible
         a.pend[X] = 0;
         a.arrive[X] = 0;
+        const int hl = child_height(t, __float_as_int(kids.x)), hr = child_height(t, __float_as_int(kids.y));
         NodeRec r = load_node_cg(t.node, X);
         int4 cc = __ldcg(t.ncnt + X);
         Box3 b = empty_box();
@@ -164,7 +169,7 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         if (!box_empty(bl)) box_union(b, bl);
         if (!box_empty(br)) box_union(b, br);
         int slots = cc.x + cc.z, del = cc.y + cc.w;
-        int h = 1 + max(child_height(t, r.left()), child_height(t, r.right()));
+        int h = 1 + max(hl, hr);
         t.nheight[X] = h;
         bool viol = false;
         if (slots > c.min_size) {
