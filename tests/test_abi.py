@@ -43,6 +43,34 @@ def test_binding_covers_every_declared_symbol():
     assert sorted(ikdg.SIGNATURES) == declared()
 
 
+def prototypes():
+    """{name: (return type, parameter count)} from include/ikdg.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for ret, name, params in re.findall(r"([A-Za-z_][\w\s\*]*?)\b(ikdg_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", text,
+                                        flags=re.S):
+        p = params.strip()
+        out[name] = (" ".join(ret.split()), 0 if p in ("", "void") else len(p.split(",")))
+    return out
+
+
+def test_binding_signatures_match_the_header():
+    # Same parameter count and the same kind of return value for every entry
+    # point: a binding out of step with the header would pass wrong arguments.
+    import ikdg
+    protos = prototypes()
+    assert sorted(protos) == declared()
+    for name, (ret, nparams) in protos.items():
+        restype, argtypes = ikdg.SIGNATURES[name]
+        assert len(argtypes) == nparams, f"{name}: {len(argtypes)} arguments bound, {nparams} declared"
+        if ret.endswith("char*") or ret.endswith("char *"):
+            assert restype is C.c_char_p, name
+        else:
+            assert ret.split()[-1] == "int" and restype is C.c_int, f"{name}: returns {ret}"
+
+
 def test_create_without_device_fails_cleanly(lib):
     import torch
     if torch.cuda.is_available():
