@@ -1565,8 +1565,9 @@ int ikdg_knn_device_noalloc(ikdg_tree* h, const float* q, int64_t nq, int32_t st
         CK(ikdg::noalloc_scratch(t.device, &scratch));
         if (ikdg::knn_temp_bytes(nq, k) > ikdg::noalloc_scratch_bytes())
             throw ikdg::Internal{"knn_device_noalloc: scratch array too small"};
-        // Always sorts the batch (bins at QBIN_BITS levels): the sort is the
-        // part that needs scratch.  Nothing here allocates.
+        // Batches of QBIN_MIN_QUERIES or more are sorted (bins at QBIN_BITS
+        // levels): the sort is the part that needs scratch.  Smaller batches
+        // run unsorted and touch no scratch.  Nothing here allocates.
         ikdg::launch_knn(t.dt, q, stride, nq, k, ikdg::max_sq_threshold(max_dist), ids, d2, xyz, cnt, scratch,
                          t.knn_lanes, ikdg::QBIN_BITS, t.stream);
         CK(cudaGetLastError());

@@ -108,20 +108,24 @@ int ikdg_knn_device(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, in
                     int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
 
 /* kNN for callers that cannot allocate device memory (no counterpart in the
- * reference).  Code that runs where cudaMalloc is off limits - inside a CUDA
- * graph capture region, in a real-time loop that must not hit the allocator,
- * or beside a framework that owns all device memory - can still search the
- * tree: this variant of ikdg_knn_device calls no cudaMalloc / cudaFree and no
- * allocating library routine.  It always sorts the batch into spatially
- * coherent order, and the sort's scratch lives in one static device array of
- * the library (about 2.7 MB, held on every GPU that loads libikdg until the
- * process exits).  Limits: nq <= 262144 queries and k <= 64 per call; larger
- * requests fail with IKDG_BAD_ARG.  The first call on a device looks the array
- * up (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the array: calls that can overlap on the GPU (for
- * example on two trees with different streams) race on it and must be
- * serialised by the caller.  Pointers are device pointers; asynchronous on
- * the tree's stream; results equal ikdg_knn_device's. */
+ * reference).  Some integrations may not call cudaMalloc while they search:
+ * a real-time loop (a LiDAR odometry step, for instance) cannot accept the
+ * device-wide synchronisation and unbounded latency a cudaMalloc / cudaFree
+ * may bring, and a host whose framework reserves and manages all device
+ * memory itself leaves no room for allocations of its own.  This variant of
+ * ikdg_knn_device calls no cudaMalloc / cudaFree and no allocating library
+ * routine.  Batches of 2,048 queries or more are sorted into spatially
+ * coherent order first, and that sort's scratch lives in one static device
+ * array of the library (about 2.7 MB, held on every GPU that loads libikdg
+ * until the process exits); smaller batches are searched unsorted and use no
+ * scratch.  Limits: nq <= 262144 queries and k <= 64 per call; larger
+ * requests fail with IKDG_BAD_ARG.  The first call on a device looks the
+ * array up (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's contents:
+ * calls that can overlap on the GPU (for example on two trees with different
+ * streams) race on it and must be serialised by the caller.  Pointers are
+ * device pointers; asynchronous on the tree's stream; results equal
+ * ikdg_knn_device's. */
 int ikdg_knn_device_noalloc(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
                             int32_t* out_ids, float* out_d2, float* out_xyz, int32_t* out_count);
 

@@ -1,10 +1,12 @@
 """The allocation-free kNN entry point (ikdg_knn_device_noalloc).
 
-Callers that cannot allocate device memory (inside a graph capture region, a
-real-time loop, or beside a framework that owns the allocator) use this
-variant; its scratch is a static device array inside libikdg.  Checked through
+Some callers may not allocate device memory while they search: real-time loops
+that cannot take an allocation's synchronisation and latency, and hosts whose
+framework reserves all device memory itself.  They use this variant, whose
+query-sort scratch is a static device array inside libikdg.  Checked through
 the C ABI against the ordinary device kNN (ikdg_knn_device), bit for bit, on
-two calls in a row (the second call reuses the scratch left by the first).
+two calls in a row (the second call reuses the scratch left by the first), for
+register-resident (k <= 8) and shared-memory (8 < k <= 64) candidate lists.
 This file is collected last so that a stop-at-first-failure run has already
 run every other test.
 """
@@ -37,7 +39,7 @@ def test_noalloc_knn_matches_device_knn_twice(ikdg_mod):
     pts = rng.uniform(-40, 40, (300000, 3)).astype(np.float32)
     tree = ikdg_mod.KDTree(device=0)
     tree.Build(pts)
-    for call, (k, md) in enumerate(((5, math.inf), (8, 2.0))):
+    for call, (k, md) in enumerate(((5, math.inf), (8, 2.0), (16, math.inf), (64, 3.0))):
         q = torch.from_numpy(rng.uniform(-41, 41, (NQ, 3)).astype(np.float32)).to(dev)
         want = _device_knn(tree, tree.knn_device, q, k, md)
         got = _device_knn(tree, tree.knn_device_noalloc, q, k, md)
