@@ -77,19 +77,24 @@ def make_queries(step: int) -> np.ndarray:
 
 
 LIDAR_MAP = 2_000_000
-LIDAR_SCANS = 12
+LIDAR_SCANS = 100
+_LIDAR = None
 
 
 def lidar_workload():
-    """The LiDAR-like mapping stream: base map, then per scan (points, boxes)."""
-    import synthetic as S
-    world = S.lidar_world(2001)
-    base = S.lidar_map(world, LIDAR_MAP, 2002)
-    scans = []
-    for s, pose in enumerate(S.trajectory(LIDAR_SCANS, 2003)):
-        pts = S.lidar_scan(world, pose, 5000 + s)
-        scans.append((pts, S.cube_complement_boxes((pose[0], pose[1], 1.8), 100.0)))
-    return base, scans
+    """The LiDAR-like mapping stream: base map, then per scan (points, boxes).
+    Generated once per process (ray casting 100 scans takes a few seconds)."""
+    global _LIDAR
+    if _LIDAR is None:
+        import synthetic as S
+        world = S.lidar_world(2001)
+        base = S.lidar_map(world, LIDAR_MAP, 2002)
+        scans = []
+        for s, pose in enumerate(S.trajectory(LIDAR_SCANS, 2003)):
+            pts = S.lidar_scan(world, pose, 5000 + s)
+            scans.append((pts, S.cube_complement_boxes((pose[0], pose[1], 1.8), 100.0)))
+        _LIDAR = (base, scans)
+    return _LIDAR
 
 
 def run_scans(tree, scans, knn):
@@ -179,6 +184,47 @@ class ClockSampler:
 MM_SEED = 3001
 STRESS_N = 20_000_000
 STRESS_Q = 1_000_000
+
+
+def range_bench(tree, torch, dev, reps: int = 3) -> dict:
+    """Box and radius search of RANGE_Q queries each on the headline map
+    through the device entry points (count pass, prefix sum, write pass),
+    CUDA events on the tree stream, median of `reps`."""
+    boxes, centres, radius = range_queries()
+    st = torch.cuda.ExternalStream(tree.stream(), device=dev)
+    b = torch.from_numpy(boxes).to(dev)
+    c = torch.from_numpy(centres).to(dev)
+    r = torch.from_numpy(radius).to(dev)
+    offs = torch.empty((RANGE_Q + 1,), dtype=torch.int64, device=dev)
+    total = torch.zeros((1,), dtype=torch.int64, device=dev)
+    out = {"workload": f"{RANGE_Q} boxes (side U(0.5,5) m per axis) and {RANGE_Q} radius queries "
+                       "(r U(0.5,5) m) on the 1M-point uniform map; ids and points out",
+           "timing": f"CUDA events on the tree stream, median of {reps}"}
+    for name, call in (("box", lambda i, cap, x: tree.box_search_device(b.data_ptr(), RANGE_Q, offs.data_ptr(), i,
+                                                                         cap, x, total.data_ptr())),
+                       ("radius", lambda i, cap, x: tree.radius_search_device(c.data_ptr(), RANGE_Q, r.data_ptr(),
+                                                                               offs.data_ptr(), i, cap, x,
+                                                                               total.data_ptr()))):
+        call(0, 0, 0)
+        tree.synchronize()
+        cap = int(total.item())
+        rid = torch.empty((max(cap, 1),), dtype=torch.int32, device=dev)
+        rxyz = torch.empty((max(cap, 1), 3), dtype=torch.float32, device=dev)
+        call(rid.data_ptr(), cap, rxyz.data_ptr())
+        tree.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            call(rid.data_ptr(), cap, rxyz.data_ptr())
+            e1.record(st)
+            tree.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = statistics.median(ts)
+        out[f"{name}_ms"] = ms
+        out[f"{name}_queries_per_s"] = RANGE_Q / (ms / 1e3)
+        out[f"{name}_hits"] = cap
+    return out
 
 
 def stress_bench(ikdg, torch, device: int, reps: int = 3) -> dict:
@@ -399,14 +445,112 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
     return out
 
 
-def cpu_baseline(pts, queries, steps: int):
-    """The oracle port (CPU restatement of the reference) on all host cores."""
-    sys.path.insert(0, ORACLE)
+CONFIG = {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K, "max_dist": "inf",
+          "l2": "GPU arm: flushed before every timed step by a 512 MB write (host arm: no flush)"}
+PARITY_SAMPLE = 2000
+RANGE_Q = 100_000
+
+
+def range_queries():
+    """Box (side U(0.5, 5) m per axis) and radius (r U(0.5, 5) m) queries
+    centred uniformly in the headline map's cube: the range-search sizes of
+    the batched multi-map workload, on the 1M-point map."""
+    rng = np.random.default_rng(7500)
+    c = rng.uniform(-EXTENT, EXTENT, (RANGE_Q, 3))
+    side = rng.uniform(0.5, 5.0, (RANGE_Q, 3))
+    boxes = np.concatenate([c - side / 2, c + side / 2], 1).astype(np.float32)
+    centres = rng.uniform(-EXTENT, EXTENT, (RANGE_Q, 3)).astype(np.float32)
+    radius = rng.uniform(0.5, 5.0, RANGE_Q).astype(np.float32)
+    return boxes, centres, radius
+
+
+def oracle_kind():
+    """The CPU implementation timed beside the GPU: the unmodified reference
+    (oracle/_ref/libikd_ref.so, compiled from the reference install in
+    baseline/_ref/) when it is there, else the oracle port."""
+    if ORACLE not in sys.path:
+        sys.path.insert(0, ORACLE)
     import oracle_lib
+    if not oracle_lib.available("ref") and os.path.isfile(
+            os.path.join(ROOT, "baseline", "_ref", "ikd-Tree", "ikd_Tree.cpp")):
+        try:
+            oracle_lib.build("ref")
+        except Exception:
+            pass
+    if oracle_lib.available("ref"):
+        return "ref"
     if not oracle_lib.available("port"):
         oracle_lib.build("port")
+    return "port"
+
+
+KIND_NAME = {"ref": "reference", "port": "port"}
+
+
+class StdoutToStderr:
+    """Sends what native code prints to stdout (the reference announces its
+    rebuild thread with printf) to stderr, so stdout carries only the JSON
+    line."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        os.dup2(2, 1)
+        return self
+
+    def __exit__(self, *exc):
+        sys.stdout.flush()
+        import ctypes
+        ctypes.CDLL(None).fflush(None)  # C stdio buffers, still on stderr's descriptor
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+
+
+def knn_rows_match(q, ref_xyz, ref_d2, ref_cnt, got_xyz, got_d2, got_cnt) -> int:
+    """Rows whose kNN result differs (counts, squared-distance bits, and the
+    neighbour points where no two distances of the row tie; tied rows accept
+    any point at the tied distance)."""
+    bad = 0
+    ref_d2 = np.asarray(ref_d2, np.float32)
+    got_d2 = np.asarray(got_d2, np.float32)
+    for i in range(len(q)):
+        c = int(ref_cnt[i])
+        if int(got_cnt[i]) != c:
+            bad += 1
+            continue
+        rd, gd = ref_d2[i, :c].view(np.uint32), got_d2[i, :c].view(np.uint32)
+        if not np.array_equal(rd, gd):
+            bad += 1
+            continue
+        if len(np.unique(rd)) == c:
+            if not np.array_equal(np.asarray(ref_xyz[i, :c], np.float32).view(np.uint32),
+                                  np.asarray(got_xyz[i, :c], np.float32).view(np.uint32)):
+                bad += 1
+            continue
+        for j in range(c):
+            p = np.asarray(got_xyz[i, j], np.float32)
+            d = (q[i][0] - p[0]) * (q[i][0] - p[0]) + (q[i][1] - p[1]) * (q[i][1] - p[1])
+            d = np.float32(np.float32(d) + np.float32((q[i][2] - p[2]) * (q[i][2] - p[2])))
+            if np.float32(d).view(np.uint32) != gd[j]:
+                bad += 1
+                break
+    return bad
+
+
+def cpu_baseline(pts, queries, steps: int, check=None, lidar_gpu=None, range_gpu=None):
+    """The CPU implementation (oracle_kind()) on this host's cores.
+
+    Times batches of the headline workload on all cores and on one thread,
+    the LiDAR mapping stream (kNN on all cores, mutations on one caller: the
+    reference's background rebuild thread runs, calls return as the
+    reference's own do), and box / radius searches on the 1M-point map on all
+    cores.  `check` = (queries, xyz, d2, cnt) of GPU rows: compared row by row
+    with the CPU implementation's rows on the same queries."""
+    sys.path.insert(0, ORACLE)
+    import oracle_lib
+    kind = oracle_kind()
     cores = os.cpu_count() or 1
-    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind="port")
+    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind=kind)
     t.Build(pts)
     t.knn(queries[0][:1000], K, nthreads=cores)
     times = []
@@ -422,40 +566,80 @@ def cpu_baseline(pts, queries, steps: int):
         t.knn(queries[s % len(queries)][:20000], K, nthreads=1)
         t1.append(time.perf_counter() - t0)
     qps_1 = 20000 / statistics.median(t1)
+    out = {"value": qps, "unit": "queries/s", "cores": cores, "kind": KIND_NAME[kind], "value_1_thread": qps_1,
+           "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries "
+                     f"(1 thread: 20k-query slices); {LIDAR_SCANS} LiDAR scans on the {LIDAR_MAP}-point map; "
+                     f"{RANGE_Q} box and {RANGE_Q} radius queries on the 1M map"}
+    if check is not None:
+        cq, gx, gd, gc = check
+        rx, rd, rc = t.knn(cq, K, nthreads=cores)
+        bad = knn_rows_match(cq, rx, rd, rc, gx, gd, gc)
+        out["parity_sample"] = {"rows": len(cq), "rows_differing": bad, "against": KIND_NAME[kind]}
+    # box / radius search on all cores
+    boxes, centres, radius = range_queries()
+    t0 = time.perf_counter()
+    offs_b, _ = t.box_search(boxes, nthreads=cores)
+    box_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    offs_r, _ = t.radius_search(centres, radius, nthreads=cores)
+    rad_s = time.perf_counter() - t0
+    out["range"] = {"box_queries_per_s": RANGE_Q / box_s, "radius_queries_per_s": RANGE_Q / rad_s,
+                    "box_hits": int(offs_b[-1]), "radius_hits": int(offs_r[-1])}
+    if range_gpu is not None:
+        out["range"]["hits_match_gpu"] = (int(offs_b[-1]) == range_gpu["box_hits"]
+                                          and int(offs_r[-1]) == range_gpu["radius_hits"])
     t.close()
     # LiDAR mapping stream: kNN over all cores, mutations on one caller (the
-    # reference's mutations are single-caller).
+    # reference's mutations are single-caller); caller-visible times.
     base, scans = lidar_workload()
-    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind="port")
+    t = oracle_lib.OracleTree(0.5, 0.6, DS, kind=kind)
     t.Build(base)
+    t.set_async(True)
     upd = run_scans(t, scans, lambda p: t.knn(p, K, 5.0, nthreads=cores))
+    t.set_async(False)
+    upd["final_validnum"] = t.validnum()
+    if lidar_gpu is not None:
+        upd["final_validnum_matches_gpu"] = upd["final_validnum"] == lidar_gpu
     t.close()
-    return {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port", "value_1_thread": qps_1,
-            "sample": f"{steps} batches of {N_Q} kNN queries (k={K}) on the 1M map, OpenMP over queries; "
-                      f"{LIDAR_SCANS} LiDAR scans on the {LIDAR_MAP}-point map",
-            **upd}
+    out.update(upd)
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the CPU implementation alone, on all host cores,
+    one step = one 100k-query batch of the headline workload."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
+    sys.path.insert(0, ORACLE)
+    import oracle_lib
+    kind = oracle_kind()
+    cores = os.cpu_count() or 1
     pts = make_map()
-    steps = max(1, min(args.steps, 5))
-    queries = [make_queries(s) for s in range(steps)]
-    cb = cpu_baseline(pts, queries, steps)
+    with StdoutToStderr():
+        t = oracle_lib.OracleTree(0.5, 0.6, DS, kind=kind)
+        t.Build(pts)
+        for s in range(args.warmup):
+            t.knn(make_queries(s), K, nthreads=cores)
+        times = []
+        for s in range(args.steps):
+            q = make_queries(args.warmup + s)
+            t0 = time.perf_counter()
+            t.knn(q, K, nthreads=cores)
+            times.append(time.perf_counter() - t0)
+        t.close()
+    ms = 1e3 * statistics.mean(times)
+    value = N_Q / (ms / 1e3)
     line = {
-        "metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": args.gpus, "steps": steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * N_Q / cb["value"], "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K,
-                   "max_dist": "inf"},
+        "config": dict(CONFIG),
         "impl": "reference",
-        "cpu_baseline": {"value": cb["value"], "unit": "queries/s", "cores": cb["cores"], "kind": cb["kind"],
-                         "sample": cb["sample"]},
-        "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "update_ms_per_scan": cb["update_ms_per_scan"], "update_ms_first_scan": cb["update_ms_first_scan"],
-        "scan_knn_ms": cb["scan_knn_ms"],
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": KIND_NAME[kind],
+                         "sample": f"{args.steps} timed batches of {N_Q} kNN queries (k={K}) on the 1M map, "
+                                   f"OpenMP over Nearest_Search calls on {cores} threads"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -529,6 +713,12 @@ def run_ours(args):
     barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = statistics.mean(step_ms)
+    # rows of the last timed step, checked against the CPU implementation in
+    # the cpu_baseline leg
+    last_q = qhost[W + Kst - 1][:PARITY_SAMPLE]
+    last_ids = ids[:PARITY_SAMPLE].cpu().numpy()
+    parity_rows = (last_q, xyz[:PARITY_SAMPLE].cpu().numpy(), d2[:PARITY_SAMPLE].cpu().numpy(),
+                   (last_ids >= 0).sum(1))
 
     # ---- e2e: pinned host buffers through the C ABI (ikdg_knn): the queries
     # come from host memory and ids, squared distances, points and counts go
@@ -560,7 +750,11 @@ def run_ours(args):
     lt = ikdg.KDTree(0.5, 0.6, DS, device=local)
     lt.Build(base)
     lidar = run_scans(lt, scans, lambda p: lt.knn(p, K, 5.0, want_xyz=True))
+    lidar["final_validnum"] = lt.validnum()
     lt.close()
+
+    # ---- box / radius search on the headline map (device buffers)
+    rng_gpu = range_bench(tree, torch, dev)
 
     # ---- batched multi-map workload, scale stress
     batched = None if args.no_batch else multimap_bench(ikdg, torch, local)
@@ -574,8 +768,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": Kst, "warmup": W,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "map_points": N_MAP, "queries_per_step": N_Q, "k": K, "max_dist": "inf",
-                   "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
+        "config": dict(CONFIG),
+        "parallelism": f"replicas x{world}",
         "e2e": {"value": e2e_value, "unit": "queries/s", "ms_per_step": e2e_step,
                 "h2d_bytes_per_step": N_Q * 12, "d2h_bytes_per_step": N_Q * K * (4 + 4 + 12) + N_Q * 4,
                 "host_buffers": "pinned"},
@@ -590,13 +784,26 @@ def run_ours(args):
         "update": {"workload": f"lidar map {LIDAR_MAP} pts, {LIDAR_SCANS} scans of ~{lidar['scan_points']} pts, "
                                "0.5 m downsampling, 200 m sliding cube", **lidar},
         "wall_s_timed_region": t_wall,
+        "range": rng_gpu,
     }
     if batched is not None:
         line["batched"] = batched
     if stress is not None:
         line["stress"] = stress
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(pts, qhost[:3], 3)
+        with StdoutToStderr():
+            cb = cpu_baseline(pts, qhost[:3], 3, check=parity_rows, lidar_gpu=lidar["final_validnum"],
+                              range_gpu=rng_gpu)
+        line["cpu_baseline"] = cb
+        ps = cb.get("parity_sample")
+        line["parity_sample_ok"] = ps is not None and ps["rows_differing"] == 0
+        line["update"]["cpu_ms_per_scan"] = cb["update_ms_per_scan"]
+        line["update"]["final_validnum_matches_cpu"] = cb.get("final_validnum_matches_gpu")
+        rng_gpu["cpu_box_queries_per_s"] = cb["range"]["box_queries_per_s"]
+        rng_gpu["cpu_radius_queries_per_s"] = cb["range"]["radius_queries_per_s"]
+        rng_gpu["box_ratio_vs_cpu"] = rng_gpu["box_queries_per_s"] / cb["range"]["box_queries_per_s"]
+        rng_gpu["radius_ratio_vs_cpu"] = rng_gpu["radius_queries_per_s"] / cb["range"]["radius_queries_per_s"]
+        rng_gpu["hits_match_cpu"] = cb["range"].get("hits_match_gpu")
     if rank == 0:
         print(json.dumps(line), flush=True)
     tree.close()

@@ -100,18 +100,22 @@ def lidar_scan(world: World, pose, seed: int, beams: int = 32, azimuths: int = 6
     gx = o[0] + t * d[:, 0]
     gy = o[1] + t * d[:, 1]
     t[(np.abs(gx) > world.half) | (np.abs(gy) > world.half)] = np.inf
-    # walls: vertical rectangles, normal n = (-sin, cos, 0)
-    nx, ny = -np.sin(world.wall_yaw), np.cos(world.wall_yaw)
-    ux, uy = np.cos(world.wall_yaw), np.sin(world.wall_yaw)
+    # walls: vertical rectangles, normal n = (-sin, cos, 0).  A wall whose
+    # nearest point lies beyond max_range can only give hits that are dropped
+    # below, so it is left out of the intersection (same output, less work).
+    near = np.hypot(world.wall_c[:, 0] - o[0], world.wall_c[:, 1] - o[1]) - world.wall_len / 2 <= max_range
+    wc, wyaw, wlen, wh = world.wall_c[near], world.wall_yaw[near], world.wall_len[near], world.wall_h[near]
+    nx, ny = -np.sin(wyaw), np.cos(wyaw)
+    ux, uy = np.cos(wyaw), np.sin(wyaw)
     denom = d[:, 0:1] * nx[None] + d[:, 1:2] * ny[None]                  # [R, W]
-    num = (world.wall_c[:, 0] - o[0]) * nx + (world.wall_c[:, 1] - o[1]) * ny  # [W]
+    num = (wc[:, 0] - o[0]) * nx + (wc[:, 1] - o[1]) * ny  # [W]
     with np.errstate(divide="ignore", invalid="ignore"):
         tw = num[None] / denom
     hx = o[0] + tw * d[:, 0:1]
     hy = o[1] + tw * d[:, 1:2]
     hz = o[2] + tw * d[:, 2:3]
-    along = (hx - world.wall_c[:, 0]) * ux + (hy - world.wall_c[:, 1]) * uy
-    ok = (tw > 0) & (np.abs(along) <= world.wall_len / 2) & (hz >= 0) & (hz <= world.wall_h)
+    along = (hx - wc[:, 0]) * ux + (hy - wc[:, 1]) * uy
+    ok = (tw > 0) & (np.abs(along) <= wlen / 2) & (hz >= 0) & (hz <= wh)
     tw = np.where(ok, tw, np.inf).min(1)
     t = np.minimum(t, tw)
     keep = (t >= 1.0) & (t <= max_range)

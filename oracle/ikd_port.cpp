@@ -718,6 +718,8 @@ int ora_size(void* hp) { return ((Handle*)hp)->tree->size(); }
 int ora_validnum(void* hp) { return ((Handle*)hp)->tree->validnum(); }
 void ora_settle(void*) {}
 
+void ora_set_async(void*, int) {}
+
 int ora_acquire_removed(void* hp) {
     Handle* h = (Handle*)hp;
     h->removed.clear();

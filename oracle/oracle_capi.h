@@ -40,6 +40,13 @@ int ora_flatten(void* h, float* out_xyz, int cap);
 int ora_size(void* h);
 int ora_validnum(void* h);
 void ora_settle(void* h);
+// async = 1: mutations and searches run as the reference's own calls do,
+// without waiting for its background rebuild thread (timing the caller-visible
+// cost; the reference lets searches run during a rebuild, ikd_Tree.cpp:875-884);
+// flatten / size / validnum / removed points still wait for it.  async = 0 (default): every mutation waits for
+// the rebuild thread before and after, so results are deterministic.  The
+// port has no background thread; it accepts the call and ignores it.
+void ora_set_async(void* h, int async);
 int ora_acquire_removed(void* h);  // drains into a staging buffer, returns its size
 void ora_fetch_removed(void* h, float* out_xyz);
 void ora_tree_range(void* h, float* box6);

@@ -64,6 +64,7 @@ def _lib(kind: str) -> C.CDLL:
         "ora_size": (C.c_int, [C.c_void_p]),
         "ora_validnum": (C.c_int, [C.c_void_p]),
         "ora_settle": (None, [C.c_void_p]),
+        "ora_set_async": (None, [C.c_void_p, C.c_int]),
         "ora_acquire_removed": (C.c_int, [C.c_void_p]),
         "ora_fetch_removed": (None, [C.c_void_p, _fp]),
         "ora_tree_range": (None, [C.c_void_p, _fp]),
@@ -164,6 +165,14 @@ class OracleTree:
         if n:
             self.lib.ora_flatten(self.h, _p(out), n)
         return out
+
+    def set_async(self, on: bool):
+        """Timing mode: calls return without waiting for the reference's
+        background rebuild thread (a no-op for the port)."""
+        self.lib.ora_set_async(self.h, int(bool(on)))
+
+    def settle(self):
+        self.lib.ora_settle(self.h)
 
     def size(self) -> int:
         return self.lib.ora_size(self.h)

@@ -35,6 +35,7 @@ struct Handle {
     Tree* tree;
     std::vector<PV> results;  // last box / radius search, per query
     PV removed;
+    bool async = false;       // mutations skip the settle (timing mode)
 };
 
 PV to_pv(const float* xyz, int n) {
@@ -85,43 +86,43 @@ void ora_build(void* hp, const float* xyz, int n) {
 
 int ora_add_points(void* hp, const float* xyz, int n, int ds) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     if (h->tree->Root_Node == nullptr) return -1;
     PV v = to_pv(xyz, n);
     int r = h->tree->Add_Points(v, ds != 0);
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     return r;
 }
 
 void ora_delete_points(void* hp, const float* xyz, int n) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     PV v = to_pv(xyz, n);
     h->tree->Delete_Points(v);
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
 }
 
 int ora_delete_boxes(void* hp, const float* boxes, int m) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     auto v = to_boxes(boxes, m);
     int r = h->tree->Delete_Point_Boxes(v);
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     return r;
 }
 
 void ora_add_boxes(void* hp, const float* boxes, int m) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     auto v = to_boxes(boxes, m);
     h->tree->Add_Point_Boxes(v);
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
 }
 
 void ora_knn(void* hp, const float* q, int nq, int k, double max_dist, float* out_xyz, float* out_d2,
              int* out_cnt, int nthreads) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     Tree* t = h->tree;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads > 0 ? nthreads : 1)
     for (int i = 0; i < nq; ++i) {
@@ -142,7 +143,7 @@ void ora_knn(void* hp, const float* q, int nq, int k, double max_dist, float* ou
 
 long long ora_box_search(void* hp, const float* boxes, int nb, long long* counts, int nthreads) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     auto bv = to_boxes(boxes, nb);
     h->results.assign(nb, PV());
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
@@ -158,7 +159,7 @@ long long ora_box_search(void* hp, const float* boxes, int nb, long long* counts
 long long ora_radius_search(void* hp, const float* q, const float* r, int nq, long long* counts,
                             int nthreads) {
     Handle* h = (Handle*)hp;
-    settle(h->tree);
+    if (!h->async) settle(h->tree);
     h->results.assign(nq, PV());
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
     for (int i = 0; i < nq; ++i) {
@@ -211,6 +212,8 @@ int ora_validnum(void* hp) {
 }
 
 void ora_settle(void* hp) { settle(((Handle*)hp)->tree); }
+
+void ora_set_async(void* hp, int async) { ((Handle*)hp)->async = async != 0; }
 
 int ora_acquire_removed(void* hp) {
     Handle* h = (Handle*)hp;

@@ -154,6 +154,14 @@ class SpecTree:
     def valid_points(self):
         return self.pts[self.valid], self.ids[self.valid]
 
+    def tree_range(self) -> np.ndarray:
+        """AABB {min xyz, max xyz} of the valid points (the root's range,
+        ikd_Tree.cpp:99-126); zeros for a tree without valid points."""
+        v = self.valid_points()[0]
+        if len(v) == 0:
+            return np.zeros(6, F32)
+        return np.concatenate([v.min(0), v.max(0)]).astype(F32)
+
     def validnum(self) -> int:
         return int(self.valid.sum())
 

@@ -24,3 +24,14 @@ def ikdg_mod():
     import ikdg
     ikdg.load()
     return ikdg
+
+
+@pytest.fixture(scope="session")
+def cpu_kinds():
+    """CPU implementations to compare against: the unmodified reference when
+    its library was built (oracle/_ref, from the reference install), and the
+    oracle port, which always builds."""
+    import oracle_lib
+    if not oracle_lib.available("port"):
+        oracle_lib.build("port")
+    return (["ref"] if oracle_lib.available("ref") else []) + ["port"]

@@ -4,8 +4,9 @@ from the reference checkout) on small seeded inputs.
 
 The reference ships no tests or golden vectors of its own, so these fixtures are
 the pin: the oracle port, the numpy model and the GPU library are all checked
-against them.  Regenerate with:  python tests/golden/make_golden.py
-(needs the reference sources; the GPU machine only reads the .npz files).
+against them.  Regenerate with:  python tests/golden/make_golden.py [names]
+(needs the reference library built from the reference sources; the GPU
+tests only read the .npz files).
 """
 from __future__ import annotations
 
@@ -149,11 +150,89 @@ def edge_fixture():
     return out
 
 
+def restore_fixture():
+    """Add_Point_Boxes, acquire_removed_points, tree_range and root_alpha
+    (ikd_Tree.cpp:491-511, :762-815, :558-571, :99-126, :148-165).
+
+    Both phases are laid out so that the reference's result does not depend on
+    its tree shape:
+    * phase A (delete_param 0.5): sparse point deletions, thin slab deletions
+      and a downsampled insertion that downsample-deletes about half of 300
+      stored points; nothing is dense enough to trigger a rebuild (size()
+      stays the number of stored points), so every deleted point is still
+      stored when one box covering all space restores them.  Points removed
+      by downsampling stay deleted.
+    * phase B (delete_param 0, a tree of 1,400 points, so that every rebuild
+      runs inline): every subtree that holds a deleted point violates the
+      delete criterion, so rebuilds purge every deleted point and
+      acquire_removed_points returns all point- and box-deleted ones (not the
+      downsample-deleted ones)."""
+    rng = np.random.default_rng(15)
+    L = 50.0
+    base = rng.uniform(-L, L, (100000, 3)).astype(F32)
+    out = {"base": base}
+    t = oracle_lib.OracleTree(0.5, 0.6, 0.2, kind="ref")
+    t.Build(base)
+    out["a_range_built"] = t.tree_range()
+    # (root_alpha right after Build is not recorded: BuildTree never sets the
+    # root's alpha fields, ikd_Tree.cpp:573-622, so they hold whatever the
+    # allocation held)
+    dp = base[rng.choice(len(base), 1500, replace=False)]
+    t.Delete_Points(dp)
+    xs = rng.uniform(-L, L, 4)
+    slabs = np.array([[x, -100, -100, x + 0.3, 100, 100] for x in xs], F32)
+    out["a_delpts"], out["a_slabs"] = dp, slabs
+    out["a_slab_ret"] = np.int64(t.Delete_Point_Boxes(slabs))
+    near = base[rng.choice(len(base), 300, replace=False)] + F32(0.001)
+    out["a_dsadd"] = near.astype(F32)
+    out["a_dsadd_ret"] = np.int64(t.Add_Points(near.astype(F32), True))
+    out["a_size"] = np.int64(t.size())
+    out["a_validnum"] = np.int64(t.validnum())
+    out["a_range"] = t.tree_range()
+    out["a_alpha"] = np.array(t.root_alpha(), F32)
+    everything = np.array([[-1e9, -1e9, -1e9, 1e9, 1e9, 1e9]], F32)
+    t.Add_Point_Boxes(everything)
+    out["a_restored_size"] = np.int64(t.size())
+    out["a_restored_validnum"] = np.int64(t.validnum())
+    out["a_restored_valid"] = t.flatten()
+    out["a_removed"] = t.acquire_removed_points()
+    # phase B: a tree below the reference's background-rebuild size (1,500
+    # points, ikd_Tree.h:15), so every rebuild runs inline and the result
+    # does not depend on thread timing
+    t.close()
+    base_b = rng.uniform(-10, 10, (1400, 3)).astype(F32)
+    out["b_base"] = base_b
+    t = oracle_lib.OracleTree(0.0, 0.6, 0.2, kind="ref")
+    t.Build(base_b)
+    near_b = base_b[rng.choice(len(base_b), 60, replace=False)] + F32(0.001)
+    out["b_dsadd"] = near_b.astype(F32)
+    out["b_dsadd_ret"] = np.int64(t.Add_Points(near_b.astype(F32), True))
+    cur = t.flatten()
+    dpb = cur[rng.choice(len(cur), 100, replace=False)]
+    t.Delete_Points(dpb)
+    bb = boxes(rng, 2, -10, 10, 4, 8)
+    out["b_delpts"], out["b_boxes"] = dpb, bb
+    out["b_box_ret"] = np.int64(t.Delete_Point_Boxes(bb))
+    out["b_removed"] = t.acquire_removed_points()
+    out["b_size"] = np.int64(t.size())
+    out["b_validnum"] = np.int64(t.validnum())
+    out["b_valid"] = t.flatten()
+    out["b_range"] = t.tree_range()
+    out["b_alpha"] = np.array(t.root_alpha(), F32)
+    t.close()
+    assert out["a_size"] == len(base) + out["a_dsadd_ret"], "phase A triggered a rebuild"
+    assert out["b_size"] == out["b_validnum"], "phase B left deleted points stored"
+    return out
+
+
 def main():
     if not oracle_lib.available("ref"):
         oracle_lib.build("ref")
+    only = sys.argv[1:]
     for name, fn in (("knn", knn_fixture), ("ops", ops_fixture), ("downsample", downsample_fixture),
-                     ("edge", edge_fixture)):
+                     ("edge", edge_fixture), ("restore", restore_fixture)):
+        if only and name not in only:
+            continue
         data = fn()
         np.savez_compressed(os.path.join(HERE, f"golden_{name}.npz"), **data)
         print("wrote", name, sum(v.nbytes for v in data.values() if hasattr(v, "nbytes")), "bytes")

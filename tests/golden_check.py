@@ -60,6 +60,31 @@ def check_knn_rows(q, ref_xyz, ref_d2, ref_cnt, got_xyz, got_d2, got_cnt):
         assert np.all(bits(sq_dist(q[i], tied)) == bits(last)), f"query {i}: tie point at wrong distance"
 
 
+def check_knn_rows_bulk(q, ref_xyz, ref_d2, ref_cnt, got_xyz, got_d2, got_cnt):
+    """check_knn_rows for large batches: counts and distance bits are compared
+    for all rows at once, points position by position in rows without two
+    equal distances (both sides list a row in ascending distance), and the
+    few rows with ties go through check_knn_rows."""
+    ref_cnt = np.asarray(ref_cnt)
+    assert np.array_equal(np.asarray(got_cnt), ref_cnt), "counts differ"
+    k = np.asarray(ref_d2).shape[1]
+    live = np.arange(k)[None, :] < ref_cnt[:, None]
+    rd = np.where(live, bits(ref_d2), 0)
+    gd = np.where(live, bits(got_d2), 0)
+    bad = np.nonzero((rd != gd).any(1))[0]
+    assert len(bad) == 0, f"squared distances differ in {len(bad)} rows, first {bad[:5]}"
+    tie = (live[:, 1:] & (rd[:, 1:] == rd[:, :-1])).any(1)
+    rx = np.where(live[..., None], bits(ref_xyz).reshape(live.shape + (3,)), 0)
+    gx = np.where(live[..., None], bits(got_xyz).reshape(live.shape + (3,)), 0)
+    bad = np.nonzero(~tie & (rx != gx).any((1, 2)))[0]
+    assert len(bad) == 0, f"neighbours differ in {len(bad)} rows, first {bad[:5]}"
+    rows = np.nonzero(tie)[0]
+    if len(rows):
+        check_knn_rows(np.asarray(q)[rows], np.asarray(ref_xyz)[rows], np.asarray(ref_d2)[rows], ref_cnt[rows],
+                       np.asarray(got_xyz)[rows], np.asarray(got_d2)[rows], np.asarray(got_cnt)[rows])
+    return len(rows)
+
+
 def check_csr(ref_offs, ref_xyz, got_offs, got_xyz):
     assert np.array_equal(np.asarray(ref_offs, np.int64), np.asarray(got_offs, np.int64)), "hit counts differ"
     for i in range(len(ref_offs) - 1):
@@ -131,6 +156,7 @@ def replay_knn_fixture(make_tree):
     check_csr(g["box_offs"], g["box_xyz"], *t.box_search(g["box"]))
     check_csr(g["rad_offs"], g["rad_xyz"], *t.radius_search(g["rad_c"], g["rad_r"]))
     assert t.validnum() == int(g["validnum"])
+    assert np.array_equal(bits(t.tree_range()), bits(g["tree_range"])), "tree_range differs"
 
 
 def replay_ops_fixture(make_tree):
@@ -185,4 +211,46 @@ def replay_edge_fixture(make_tree):
     assert np.array_equal(cnt, g["empty_cnt"]) and t.size() == int(g["empty_size"])
 
 
+def replay_restore_fixture(make_tree):
+    """Add_Point_Boxes, acquire_removed_points, tree_range and root_alpha
+    against the reference (see make_golden.restore_fixture for why these
+    sequences do not depend on the reference's tree shape)."""
+    g = load("restore")
+    everything = np.array([[-1e9, -1e9, -1e9, 1e9, 1e9, 1e9]], np.float32)
+    t = make_tree(0.5, 0.6, 0.2)
+    t.Build(g["base"])
+    assert np.array_equal(bits(t.tree_range()), bits(g["a_range_built"])), "tree_range after Build"
+    t.Delete_Points(g["a_delpts"])
+    assert t.Delete_Point_Boxes(g["a_slabs"]) == int(g["a_slab_ret"]), "slab deletion count"
+    assert t.Add_Points(g["a_dsadd"], True) == int(g["a_dsadd_ret"]), "downsampled insert count"
+    assert t.size() == int(g["a_size"]), "size(): a rebuild ran where the reference ran none"
+    assert t.validnum() == int(g["a_validnum"])
+    assert np.array_equal(bits(t.tree_range()), bits(g["a_range"])), "tree_range after deletions"
+    bal, dele = t.root_alpha()
+    # alpha_del = deleted / stored at the root: the same counts, the same
+    # float division.  alpha_bal depends on the shape (the reference's root
+    # holds one point of its own), so it is compared loosely.
+    assert np.float32(dele) == np.float32(g["a_alpha"][1]), "root alpha_del"
+    assert abs(bal - float(g["a_alpha"][0])) < 5e-3, "root alpha_bal"
+    t.Add_Point_Boxes(everything)
+    assert t.size() == int(g["a_restored_size"])
+    assert t.validnum() == int(g["a_restored_validnum"]), "validnum after Add_Point_Boxes"
+    assert same_point_set(g["a_restored_valid"], t.flatten()), "valid set after Add_Point_Boxes"
+    assert len(t.acquire_removed_points()) == len(g["a_removed"]) == 0
+    t = make_tree(0.0, 0.6, 0.2)
+    t.Build(g["b_base"])
+    assert t.Add_Points(g["b_dsadd"], True) == int(g["b_dsadd_ret"])
+    t.Delete_Points(g["b_delpts"])
+    assert t.Delete_Point_Boxes(g["b_boxes"]) == int(g["b_box_ret"])
+    assert same_point_set(g["b_removed"], t.acquire_removed_points()), "acquire_removed_points multiset"
+    assert len(t.acquire_removed_points()) == 0, "acquire_removed_points drains"
+    assert t.size() == int(g["b_size"]) and t.validnum() == int(g["b_validnum"])
+    assert same_point_set(g["b_valid"], t.flatten())
+    assert np.array_equal(bits(t.tree_range()), bits(g["b_range"])), "tree_range after purges"
+    assert np.float32(t.root_alpha()[1]) == np.float32(g["b_alpha"][1]) == 0
+
+
 REPLAYS = [replay_knn_fixture, replay_ops_fixture, replay_downsample_fixture, replay_edge_fixture]
+# Fixtures that need the whole tree API (the numpy model has no removed-point
+# record or re-insertion): run against the port and the GPU library.
+REPLAYS_TREE = REPLAYS + [replay_restore_fixture]

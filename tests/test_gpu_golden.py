@@ -8,6 +8,6 @@ import golden_check as G
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("replay", G.REPLAYS, ids=lambda f: f.__name__)
+@pytest.mark.parametrize("replay", G.REPLAYS_TREE, ids=lambda f: f.__name__)
 def test_gpu_reproduces_reference_fixtures(ikdg_mod, replay):
     replay(lambda d, b, box: G.Adapter(ikdg_mod.KDTree(d, b, box), "gpu"))

@@ -25,7 +25,7 @@ def spec_tree(d, b, box):
     return G.Adapter(spec.SpecTree(box), "spec")
 
 
-@pytest.mark.parametrize("replay", G.REPLAYS, ids=lambda f: f.__name__)
+@pytest.mark.parametrize("replay", G.REPLAYS_TREE, ids=lambda f: f.__name__)
 def test_port_reproduces_reference_fixtures(port_lib, replay):
     replay(port_tree)
 
