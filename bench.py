@@ -227,6 +227,23 @@ def range_bench(tree, torch, dev, reps: int = 3) -> dict:
     return out
 
 
+def facade_bench(threads: int = 8) -> dict:
+    """Per-point Nearest_Search through the C++ drop-in facade: the call
+    shape of a front end that searches point by point, on one thread and on
+    `threads` threads (ikd-tree_gb300/facade_latency.cpp)."""
+    exe = os.path.join(tempfile.mkdtemp(), "facade_latency")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+           os.path.join(PKG, "facade_latency.cpp"), "-o", exe, "-L", PKG, "-likdg", f"-Wl,-rpath,{PKG}",
+           "-L/usr/local/cuda/lib64", "-lcudart", "-pthread"]
+    try:
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        r = subprocess.run([exe, str(N_MAP), "20000", str(threads)], check=True, capture_output=True, text=True,
+                           timeout=600)
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except (subprocess.SubprocessError, OSError, ValueError) as e:
+        return {"error": str(e)[:300]}
+
+
 def stress_bench(ikdg, torch, device: int, reps: int = 3) -> dict:
     """Scale stress: 20M-point map, 1M-query batches, 1000 box deletions."""
     import synthetic as S
@@ -755,6 +772,8 @@ def run_ours(args):
 
     # ---- box / radius search on the headline map (device buffers)
     rng_gpu = range_bench(tree, torch, dev)
+    # ---- per-point calls through the C++ facade (own process, same GPU)
+    facade = facade_bench() if world == 1 else None
 
     # ---- batched multi-map workload, scale stress
     batched = None if args.no_batch else multimap_bench(ikdg, torch, local)
@@ -785,6 +804,7 @@ def run_ours(args):
                                "0.5 m downsampling, 200 m sliding cube", **lidar},
         "wall_s_timed_region": t_wall,
         "range": rng_gpu,
+        "facade_per_point": facade,
     }
     if batched is not None:
         line["batched"] = batched
@@ -804,6 +824,10 @@ def run_ours(args):
         rng_gpu["box_ratio_vs_cpu"] = rng_gpu["box_queries_per_s"] / cb["range"]["box_queries_per_s"]
         rng_gpu["radius_ratio_vs_cpu"] = rng_gpu["radius_queries_per_s"] / cb["range"]["radius_queries_per_s"]
         rng_gpu["hits_match_cpu"] = cb["range"].get("hits_match_gpu")
+        if facade and "us_per_call_1_thread" in facade:
+            facade["cpu_us_per_call_1_thread"] = 1e6 / cb["value_1_thread"]
+            facade["cpu_calls_per_s_all_cores"] = cb["value"]
+            facade["cpu_cores"] = cb["cores"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     tree.close()

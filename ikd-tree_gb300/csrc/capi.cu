@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <shared_mutex>
 #include <string>
 #include <vector>
 
@@ -193,7 +194,12 @@ struct Tree {
     long long next_id = 0;
     int list_cap = 0;
 
-    std::mutex mu;
+    // Calls that change or stage through the tree's own buffers hold `mu`
+    // exclusively; small host-pointer kNN calls hold it shared and run on
+    // search contexts of their own (below), so concurrent Nearest_Search
+    // callers (ikd_Tree.cpp:875-884) search at the same time.
+    std::shared_mutex mu;
+    std::mutex err_mu;
     std::string err;
     // IKDG_DEBUG_VALIDATE=1: check the whole tree's structure after every
     // mutation (slow; for tests and debugging).
@@ -226,6 +232,7 @@ struct Tree {
     }
 
     void destroy() {
+        destroy_ctxs();
         if (stream != nullptr) cudaStreamSynchronize(stream);
         free_array(dt.node);
         free_array(dt.ncnt);
@@ -661,6 +668,121 @@ struct Tree {
         finish_update(nullptr, nullptr, 0);
     }
 
+    // ---- concurrent small searches ------------------------------------------------
+    // A search context: a stream, a device buffer (a status block for the
+    // kernel's error bits, the result rows, the kNN scratch) and a pinned host
+    // mirror of the status and rows, so one device-to-host copy returns
+    // everything.  Contexts are pooled per tree and reused.
+    struct SearchCtx {
+        cudaStream_t s = nullptr;
+        char* d = nullptr;
+        char* h = nullptr;
+        size_t dcap = 0, hcap = 0;
+    };
+    std::mutex ctx_mu;
+    std::vector<SearchCtx*> ctx_free;
+    std::vector<SearchCtx*> ctx_all;
+
+    SearchCtx* take_ctx() {
+        {
+            std::lock_guard<std::mutex> l(ctx_mu);
+            if (!ctx_free.empty()) {
+                SearchCtx* c = ctx_free.back();
+                ctx_free.pop_back();
+                return c;
+            }
+        }
+        SearchCtx* c = new SearchCtx;
+        if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            throw CudaFail{cudaGetLastError(), "search stream"};
+        }
+        std::lock_guard<std::mutex> l(ctx_mu);
+        ctx_all.push_back(c);
+        return c;
+    }
+    void give_ctx(SearchCtx* c) {
+        std::lock_guard<std::mutex> l(ctx_mu);
+        ctx_free.push_back(c);
+    }
+    void destroy_ctxs() {
+        for (SearchCtx* c : ctx_all) {
+            if (c->s) cudaStreamSynchronize(c->s);
+            if (c->d) cudaFree(c->d);
+            if (c->h) cudaFreeHost(c->h);
+            if (c->s) cudaStreamDestroy(c->s);
+            delete c;
+        }
+        ctx_all.clear();
+        ctx_free.clear();
+    }
+    static void ctx_reserve(SearchCtx* c, size_t dneed, size_t hneed) {
+        if (dneed > c->dcap) {
+            if (c->d) CK(cudaFree(c->d));
+            c->d = nullptr;
+            c->dcap = 0;
+            CK(cudaMalloc(&c->d, dneed));
+            c->dcap = dneed;
+        }
+        if (hneed > c->hcap) {
+            if (c->h) CK(cudaFreeHost(c->h));
+            c->h = nullptr;
+            c->hcap = 0;
+            CK(cudaMallocHost(&c->h, hneed));
+            c->hcap = hneed;
+        }
+    }
+
+    // Host-pointer kNN of a few queries (called with `mu` held shared).  Same
+    // kernels and results as knn(); the tree is only read.
+    void knn_small(const float* q, long long nq, int stride, int k, double max_dist, int* ids, float* d2, float* xyz,
+                   int* cnt) {
+        if (nq < 0 || stride < 3 || k < 1 || (nq > 0 && (q == nullptr || ids == nullptr || d2 == nullptr)))
+            throw BadArg{"knn: bad arguments"};
+        if (nq == 0) return;
+        const size_t nk = (size_t)nq * k;
+        const size_t o_ids = align_up(sizeof(DevStatus));
+        const size_t o_d2 = o_ids + align_up(sizeof(int) * nk);
+        const size_t o_xyz = o_d2 + align_up(sizeof(float) * nk);
+        const size_t o_cnt = o_xyz + (xyz ? align_up(sizeof(float) * 3 * nk) : 0);
+        const size_t o_end = o_cnt + (cnt ? align_up(sizeof(int) * nq) : 0);
+        const size_t o_q = o_end;
+        const size_t o_tmp = o_q + (host_mode == 0 ? align_up(sizeof(float) * nq * stride) : 0);
+        const size_t dneed = o_tmp + align_up(knn_temp_bytes(nq, k) + 256);
+        const size_t hneed = std::max(o_end, o_tmp);
+        SearchCtx* c = take_ctx();
+        try {
+            ctx_reserve(c, dneed, hneed);
+            DevTree t = dt;
+            t.st = (DevStatus*)c->d;  // this call's error bits land in its own status block
+            CK(cudaMemsetAsync(c->d + offsetof(DevStatus, err), 0, sizeof(int), c->s));
+            const float* qsrc = q;
+            if (host_mode == 0) {
+                std::memcpy(c->h + o_q, q, sizeof(float) * nq * stride);
+                CK(cudaMemcpyAsync(c->d + o_q, c->h + o_q, sizeof(float) * nq * stride, cudaMemcpyHostToDevice,
+                                   c->s));
+                qsrc = (const float*)(c->d + o_q);
+            }
+            launch_knn(t, qsrc, stride, nq, k, max_sq_threshold(max_dist), (int*)(c->d + o_ids),
+                       (float*)(c->d + o_d2), xyz ? (float*)(c->d + o_xyz) : nullptr,
+                       cnt ? (int*)(c->d + o_cnt) : nullptr, c->d + o_tmp, knn_lanes, bin_bits_for(nq), c->s);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(c->h, c->d, o_end, cudaMemcpyDeviceToHost, c->s));
+            CK(cudaStreamSynchronize(c->s));
+            const DevStatus* hs = (const DevStatus*)c->h;
+            if (hs->err & ERR_STACK) throw Internal{"knn: traversal stack overflow"};
+            if (hs->err & ERR_LOOP) throw Internal{"knn: loop cap reached"};
+            std::memcpy(ids, c->h + o_ids, sizeof(int) * nk);
+            std::memcpy(d2, c->h + o_d2, sizeof(float) * nk);
+            if (xyz) std::memcpy(xyz, c->h + o_xyz, sizeof(float) * 3 * nk);
+            if (cnt) std::memcpy(cnt, c->h + o_cnt, sizeof(int) * nq);
+        } catch (...) {
+            give_ctx(c);
+            throw;
+        }
+        give_ctx(c);
+    }
+
     void knn(const float* q, long long nq, int stride, int k, double max_dist, int* ids, float* d2, float* xyz,
              int* cnt, bool device_ptrs) {
         if (nq < 0 || stride < 3 || k < 1 || (nq > 0 && (q == nullptr || ids == nullptr || d2 == nullptr)))
@@ -892,24 +1014,58 @@ struct Tree {
         }
     }
 
-    void acquire_removed(float* xyz, long long capacity, long long* n) {
+    void acquire_removed(float* xyz, int* ids, long long capacity, long long* n) {
         if (n == nullptr) throw BadArg{"acquire_removed_points: bad arguments"};
         read_status();
         long long k = std::min<long long>(st->removed_n, removed_cap);
         *n = k;
-        if (k > capacity || (k > 0 && xyz == nullptr)) throw CapacityFail{"acquire_removed_points: output too small"};
+        if (k > capacity || (k > 0 && xyz == nullptr && ids == nullptr))
+            throw CapacityFail{"acquire_removed_points: output too small"};
         if (k > 0) {
             std::vector<float4> h(k);
             CK(cudaMemcpyAsync(h.data(), removed, sizeof(float4) * k, cudaMemcpyDeviceToHost, stream));
             CK(cudaStreamSynchronize(stream));
             for (long long i = 0; i < k; ++i) {
-                xyz[3 * i] = h[i].x;
-                xyz[3 * i + 1] = h[i].y;
-                xyz[3 * i + 2] = h[i].z;
+                if (xyz) {
+                    xyz[3 * i] = h[i].x;
+                    xyz[3 * i + 1] = h[i].y;
+                    xyz[3 * i + 2] = h[i].z;
+                }
+                if (ids) {
+                    uint32_t w;
+                    std::memcpy(&w, &h[i].w, 4);
+                    ids[i] = (int)(w & ID_MASK);
+                }
             }
         }
         zero_fields(offsetof(DevStatus, removed_n), sizeof(long long));
         read_status();
+    }
+
+    // Ids the tree can still return: every stored slot (valid or deleted),
+    // then the removed points not yet acquired.
+    void live_ids(int* ids, long long capacity, long long* n) {
+        if (n == nullptr) throw BadArg{"live_ids: bad arguments"};
+        const long long stored = st->root_slots;
+        const long long rem = std::min<long long>(st->removed_n, removed_cap);
+        *n = stored + rem;
+        if (*n > capacity || (*n > 0 && ids == nullptr)) throw CapacityFail{"live_ids: output too small"};
+        if (*n == 0) return;
+        reset_counters();
+        op.ensure(align_up(sizeof(int) * std::max<long long>(stored, 1)), stream);
+        int* out = (int*)op.p;
+        if (stored > 0) launch_stored_ids(dt, out, stored, (long long*)((char*)st_dev + offsetof(DevStatus, count)),
+                                          stream);
+        if (stored > 0) CK(cudaMemcpyAsync(ids, out, sizeof(int) * stored, cudaMemcpyDeviceToHost, stream));
+        std::vector<float4> h(rem);
+        if (rem > 0) CK(cudaMemcpyAsync(h.data(), removed, sizeof(float4) * rem, cudaMemcpyDeviceToHost, stream));
+        read_status();
+        if (st->count != stored) throw Internal{"live_ids: stored slot count mismatch"};
+        for (long long i = 0; i < rem; ++i) {
+            uint32_t w;
+            std::memcpy(&w, &h[i].w, 4);
+            ids[stored + i] = (int)(w & ID_MASK);
+        }
     }
 
     void rebuild_all() {
@@ -1241,7 +1397,7 @@ struct Batch {
         if (launched) CK(cudaEventSynchronize(ev_done));
         for (size_t i = 0; i < trees.size(); ++i) {
             Tree* t = trees[i];
-            std::lock_guard<std::mutex> lock(t->mu);
+            std::unique_lock<std::shared_mutex> lock(t->mu);
             h_trees[i] = t->dt;
             h_trees[i].st = d_st;
             CK(cudaEventRecord(ev_tree[i], t->stream));
@@ -1255,7 +1411,7 @@ struct Batch {
         launched = true;
         // later work on each tree (mutations) waits for this run
         for (Tree* t : trees) {
-            std::lock_guard<std::mutex> lock(t->mu);
+            std::unique_lock<std::shared_mutex> lock(t->mu);
             CK(cudaStreamWaitEvent(t->stream, ev_done, 0));
         }
     }
@@ -1325,7 +1481,7 @@ void autotune_batch(Batch& b, int reps, const std::vector<int>& fills, const std
         try {
             for (int f : fills) {
                 {
-                    std::lock_guard<std::mutex> lock(t->mu);
+                    std::unique_lock<std::shared_mutex> lock(t->mu);
                     t->fill = f;
                     t->rebuild_all();
                 }
@@ -1342,7 +1498,7 @@ void autotune_batch(Batch& b, int reps, const std::vector<int>& fills, const std
                 }
             }
             {
-                std::lock_guard<std::mutex> lock(t->mu);
+                std::unique_lock<std::shared_mutex> lock(t->mu);
                 t->fill = best_fill;
                 t->rebuild_all();
             }
@@ -1374,14 +1530,24 @@ struct ikdg_batch {
 namespace {
 
 int fail(ikdg_tree* h, int code, const std::string& msg) {
-    if (h != nullptr) h->t.err = msg;
+    if (h != nullptr) {
+        std::lock_guard<std::mutex> l(h->t.err_mu);
+        h->t.err = msg;
+    }
     return code;
 }
 
-template <class F>
+// Runs f with the tree's lock held (exclusively, or shared for the
+// concurrent small searches) and maps exceptions to status codes.
+template <bool SHARED = false, class F>
 int guarded(ikdg_tree* h, F&& f) {
     if (h == nullptr) return IKDG_BAD_ARG;
-    std::lock_guard<std::mutex> lock(h->t.mu);
+    std::unique_lock<std::shared_mutex> xl(h->t.mu, std::defer_lock);
+    std::shared_lock<std::shared_mutex> sl(h->t.mu, std::defer_lock);
+    if (SHARED)
+        sl.lock();
+    else
+        xl.lock();
     try {
         CK(cudaSetDevice(h->t.device));
         f(h->t);
@@ -1476,7 +1642,7 @@ int ikdg_create(float delete_param, float balance_param, float box_length, int d
 int ikdg_destroy(ikdg_tree* h) {
     if (h == nullptr) return IKDG_BAD_ARG;
     {
-        std::lock_guard<std::mutex> lock(h->t.mu);
+        std::unique_lock<std::shared_mutex> lock(h->t.mu);
         cudaSetDevice(h->t.device);
         h->t.destroy();
     }
@@ -1543,6 +1709,10 @@ int ikdg_add_boxes(ikdg_tree* h, const float* boxes, int64_t m) {
 
 int ikdg_knn(ikdg_tree* h, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist, int32_t* ids,
              float* d2, float* xyz, int32_t* cnt) {
+    // A few queries with a small k (the per-point Nearest_Search of a mapping
+    // front end): concurrent callers search at the same time.
+    if (nq <= ikdg::SMALL_KNN_QUERIES && k <= ikdg::KNN_SMEM_MAX)
+        return guarded<true>(h, [&](ikdg::Tree& t) { t.knn_small(q, nq, stride, k, max_dist, ids, d2, xyz, cnt); });
     return guarded(h, [&](ikdg::Tree& t) { t.knn(q, nq, stride, k, max_dist, ids, d2, xyz, cnt, false); });
 }
 
@@ -1656,11 +1826,24 @@ int ikdg_flatten(ikdg_tree* h, float* xyz, int32_t* ids, int64_t capacity, int64
     });
 }
 
-int ikdg_acquire_removed_points(ikdg_tree* h, float* xyz, int64_t capacity, int64_t* n) {
+int ikdg_acquire_removed_points(ikdg_tree* h, float* xyz, int32_t* ids, int64_t capacity, int64_t* n) {
     return guarded(h, [&](ikdg::Tree& t) {
         long long k = 0;
         try {
-            t.acquire_removed(xyz, capacity, &k);
+            t.acquire_removed(xyz, ids, capacity, &k);
+        } catch (...) {
+            if (n) *n = k;
+            throw;
+        }
+        if (n) *n = k;
+    });
+}
+
+int ikdg_live_ids(ikdg_tree* h, int32_t* ids, int64_t capacity, int64_t* n) {
+    return guarded(h, [&](ikdg::Tree& t) {
+        long long k = 0;
+        try {
+            t.live_ids(ids, capacity, &k);
         } catch (...) {
             if (n) *n = k;
             throw;

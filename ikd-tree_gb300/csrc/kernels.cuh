@@ -65,6 +65,10 @@ constexpr int QBIN_BINS = 1 << QBIN_BITS;
 constexpr long long QBIN_MIN_QUERIES = 2048;
 constexpr long long QBIN_AUTO_QUERIES = 262144;  // default: sort batches from this size
 size_t knn_temp_bytes(long long nq, int k);
+// Host-pointer kNN calls of at most this many queries (and k <= KNN_SMEM_MAX)
+// run on pooled per-call streams with the tree's lock held shared, so
+// concurrent callers search at the same time.
+constexpr long long SMALL_KNN_QUERIES = 4096;
 // Allocation-free kNN: limit on the batch size and the device address of the
 // shared scratch array (looked up on the first call per device).
 constexpr long long NOALLOC_MAX_QUERIES = 1 << 18;

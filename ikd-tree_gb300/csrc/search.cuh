@@ -36,6 +36,13 @@ __device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4&
 #endif
 constexpr int RANGE_LEAF_BATCH = IKDG_RANGE_LEAF_BATCH;
 
+// kNN: lanes of a warp holding a leaf that end the node phase early (32: the
+// node phase runs until every lane holds a leaf or is done).
+#ifndef IKDG_KNN_LEAF_T
+#define IKDG_KNN_LEAF_T 32
+#endif
+constexpr int KNN_LEAF_T = IKDG_KNN_LEAF_T;
+
 __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
     return d < d2 || (d == d2 && id < id2);
 }
@@ -161,10 +168,13 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     };
 
     while (true) {
-        // Node phase.
+        // Node phase: ends when no lane has node work left, or when at least
+        // KNN_LEAF_T lanes hold a leaf (then those leaves are scanned while the
+        // other lanes wait, instead of the holders waiting for the longest walk).
         while (true) {
             const bool nodework = !done && cur >= 0;
             if (!__any_sync(0xffffffffu, nodework)) break;
+            if (KNN_LEAF_T < 32 && __popc(__ballot_sync(0xffffffffu, !done && cur < 0)) >= KNN_LEAF_T) break;
             if (!nodework) continue;
             if (++visits > MAX_VISITS) {
                 atomicOr(&t.st->err, ERR_LOOP);

@@ -649,6 +649,20 @@ __global__ void flatten_kernel(DevTree t, float4* __restrict__ out, long long* c
     }
 }
 
+// Ids of every stored slot (valid or deleted) of the leaves in use; slots
+// past `cap` are counted but not written.
+__global__ void stored_ids_kernel(DevTree t, int* __restrict__ out, long long cap, long long* counter) {
+    int L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= t.st->leaf_top) return;
+    if (t.lparent[L] < 0) return;
+    const int m = min(t.leaf_n[L], LEAF_CAP);
+    if (m == 0) return;
+    const long long pos = (long long)atomicAdd((unsigned long long*)counter, (unsigned long long)m);
+    const float4* lp = t.pts + (long long)L * LEAF_CAP;
+    for (int s = 0; s < m; ++s)
+        if (pos + s < cap) out[pos + s] = (int)(__float_as_uint(lp[s].w) & ID_MASK);
+}
+
 __global__ void select_root_job_kernel(DevTree t, UpdateAux a) {
     int code = __float_as_int(t.node[3].x);
     if (code == 0) return;
@@ -1241,6 +1255,11 @@ void launch_validate(const DevTree& t, const UpdateAux& a, bool at_rest, long lo
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s) {
     if (t.leaf_cap <= 0) return;
     flatten_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, out, counter);
+}
+
+void launch_stored_ids(const DevTree& t, int* out, long long cap, long long* counter, cudaStream_t s) {
+    if (t.leaf_cap <= 0) return;
+    stored_ids_kernel<<<blocks_for(t.leaf_cap, 256), 256, 0, s>>>(t, out, cap, counter);
 }
 
 void launch_select_root_job(const DevTree& t, const UpdateAux& a, cudaStream_t s) {

@@ -69,6 +69,9 @@ void launch_pack_points(const DevTree& t, const float* in, int stride, long long
 void launch_check_finite(const DevTree& t, const float* in, long long count, cudaStream_t s);
 // Copies every valid point ({x, y, z, id}) to out; *counter += count.
 void launch_flatten(const DevTree& t, float4* out, long long* counter, cudaStream_t s);
+// Writes the id of every stored slot (valid or deleted) to out[0 .. cap);
+// *counter += the number of stored slots.
+void launch_stored_ids(const DevTree& t, int* out, long long cap, long long* counter, cudaStream_t s);
 // Structural check of the whole tree; *bad += number of violations.
 // Structural check (links, counts, AABBs) plus the bookkeeping flags; at_rest
 // (between calls) also requires cleared violation / job tags and leaves within

@@ -58,7 +58,8 @@ SIGNATURES = {
     "ikdg_tree_range": (C.c_int, [_vp, _fp]),
     "ikdg_root_alpha": (C.c_int, [_vp, _fp, _fp]),
     "ikdg_flatten": (C.c_int, [_vp, _fp, _ip, C.c_int64, _lp]),
-    "ikdg_acquire_removed_points": (C.c_int, [_vp, _fp, C.c_int64, _lp]),
+    "ikdg_acquire_removed_points": (C.c_int, [_vp, _fp, _ip, C.c_int64, _lp]),
+    "ikdg_live_ids": (C.c_int, [_vp, _ip, C.c_int64, _lp]),
     "ikdg_rebuild": (C.c_int, [_vp]),
     "ikdg_debug_validate": (C.c_int, [_vp, _lp]),
     "ikdg_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
@@ -311,17 +312,33 @@ class KDTree:
             self._check(self.lib.ikdg_flatten(self.h, _p(xyz), ids.ctypes.data_as(_ip), k, C.byref(n)), "flatten")
         return (xyz[:k], ids[:k]) if with_ids else xyz[:k]
 
-    def acquire_removed_points(self) -> np.ndarray:
+    def acquire_removed_points(self, with_ids: bool = False):
         n = C.c_int64(0)
-        st = self.lib.ikdg_acquire_removed_points(self.h, None, 0, C.byref(n))
+        st = self.lib.ikdg_acquire_removed_points(self.h, None, None, 0, C.byref(n))
         if st == OK and n.value == 0:
-            return np.zeros((0, 3), np.float32)
+            empty = np.zeros((0, 3), np.float32)
+            return (empty, np.zeros(0, np.int32)) if with_ids else empty
         if st not in (OK, CAPACITY):
             self._check(st, "acquire_removed_points")
         k = n.value
         xyz = np.empty((k, 3), np.float32)
-        self._check(self.lib.ikdg_acquire_removed_points(self.h, _p(xyz), k, C.byref(n)), "acquire_removed_points")
-        return xyz
+        ids = np.empty(k, np.int32)
+        self._check(self.lib.ikdg_acquire_removed_points(self.h, _p(xyz), ids.ctypes.data_as(_ip), k, C.byref(n)),
+                    "acquire_removed_points")
+        return (xyz, ids) if with_ids else xyz
+
+    def live_ids(self) -> np.ndarray:
+        """Ids the tree can still return: stored (valid or deleted) points and
+        removed points not yet acquired."""
+        n = C.c_int64(0)
+        st = self.lib.ikdg_live_ids(self.h, None, 0, C.byref(n))
+        if st not in (OK, CAPACITY):
+            self._check(st, "live_ids")
+        k = n.value
+        ids = np.empty(max(k, 1), np.int32)
+        if k > 0:
+            self._check(self.lib.ikdg_live_ids(self.h, ids.ctypes.data_as(_ip), k, C.byref(n)), "live_ids")
+        return ids[:k]
 
     def validate(self) -> int:
         """Structural violations of the device tree (0 = sound)."""

@@ -7,10 +7,14 @@
 // the C ABI; there is no CPU code path.
 //
 // PointType needs public float members x, y, z (ikdTree_PointType,
-// pcl::PointXYZ, pcl::PointXYZI, pcl::PointXYZINormal, ...).  Searches return
-// full PointType values: the facade keeps every inserted point on the host,
-// indexed by the id the device tree assigns to it, so payload fields such as
-// intensity or normals come back exactly as they were inserted.
+// pcl::PointXYZ, pcl::PointXYZI, pcl::PointXYZINormal, ...).  Searches and
+// acquire_removed_points return full PointType values: the facade keeps the
+// inserted points on the host, keyed by the id the device tree assigns to
+// each, so payload fields such as intensity or normals come back exactly as
+// they were inserted.  Points no call can return any more (downsampling
+// losers, deleted points dropped by rebuilds and already handed out) are
+// dropped from that store whenever it holds more than twice the live ones, so
+// host memory stays proportional to the map, not to everything ever inserted.
 //
 // Differences from the reference, by design:
 //   * results at exactly tied distances are ordered by insertion id;
@@ -26,6 +30,7 @@
 // Radius_Search_Batch) run a whole set of queries in one kernel launch.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -130,7 +135,10 @@ class KD_TREE {
     void Build(PointVector point_cloud) {
         std::vector<float> xyz = pack(point_cloud);
         check(ikdg_build(t_, xyz.data(), (int64_t)point_cloud.size(), 3), "Build");
-        store_.assign(point_cloud.begin(), point_cloud.end());
+        ids_.clear();
+        pay_.clear();
+        next_id_ = 0;
+        remember(point_cloud);
         refresh_root();
     }
 
@@ -146,7 +154,7 @@ class KD_TREE {
         int32_t cnt = 0;
         check(ikdg_knn(t_, q, 1, 3, k_nearest, max_dist, ids.data(), d2.data(), nullptr, &cnt), "Nearest_Search");
         for (int j = 0; j < cnt; ++j) {
-            Nearest_Points.push_back(store_[ids[j]]);
+            Nearest_Points.push_back(payload(ids[j]));
             Point_Distance.push_back(d2[j]);
         }
     }
@@ -165,7 +173,7 @@ class KD_TREE {
               "Nearest_Search_Batch");
         for (size_t i = 0; i < nq; ++i)
             for (int j = 0; j < cnt[i]; ++j) {
-                Nearest_Points[i].push_back(store_[ids[i * k_nearest + j]]);
+                Nearest_Points[i].push_back(payload(ids[i * k_nearest + j]));
                 Point_Distance[i].push_back(d2[i * k_nearest + j]);
             }
     }
@@ -210,8 +218,9 @@ class KD_TREE {
         check(ikdg_add_points(t_, xyz.data(), (int64_t)PointToAdd.size(), 3, downsample_on ? 1 : 0, &added),
               "Add_Points");
         // The device assigned ids next .. next + n - 1 to the inputs.
-        store_.insert(store_.end(), PointToAdd.begin(), PointToAdd.end());
+        remember(PointToAdd);
         refresh_root();
+        compact();
         return (int)added;
     }
 
@@ -226,6 +235,7 @@ class KD_TREE {
         std::vector<float> xyz = pack(PointToDel);
         check(ikdg_delete_points(t_, xyz.data(), (int64_t)PointToDel.size(), 3), "Delete_Points");
         refresh_root();
+        compact();
     }
 
     // Delete_Point_Boxes, ikd_Tree.h:242.
@@ -234,6 +244,7 @@ class KD_TREE {
         int64_t n = 0;
         check(ikdg_delete_boxes(t_, b.data(), (int64_t)BoxPoints.size(), &n), "Delete_Point_Boxes");
         refresh_root();
+        compact();
         return (int)n;
     }
 
@@ -254,25 +265,25 @@ class KD_TREE {
         std::vector<int32_t> ids(n);
         check(ikdg_flatten(t_, nullptr, ids.data(), n, &n), "flatten");
         Storage.reserve(n);
-        for (int64_t i = 0; i < n; ++i) Storage.push_back(store_[ids[i]]);
+        for (int64_t i = 0; i < n; ++i) Storage.push_back(payload(ids[i]));
     }
 
-    // acquire_removed_points, ikd_Tree.h:244 (coordinates of the removed points).
+    // acquire_removed_points, ikd_Tree.h:244: the removed points as inserted
+    // (payload fields included).
     void acquire_removed_points(PointVector& removed_points) {
         int64_t n = 0;
-        int st = ikdg_acquire_removed_points(t_, nullptr, 0, &n);
+        int st = ikdg_acquire_removed_points(t_, nullptr, nullptr, 0, &n);
         if (st != IKDG_OK && st != IKDG_CAPACITY) check(st, "acquire_removed_points");
         if (n == 0) return;
-        std::vector<float> xyz(3 * n);
-        check(ikdg_acquire_removed_points(t_, xyz.data(), n, &n), "acquire_removed_points");
-        for (int64_t i = 0; i < n; ++i) {
-            PointType p{};
-            p.x = xyz[3 * i];
-            p.y = xyz[3 * i + 1];
-            p.z = xyz[3 * i + 2];
-            removed_points.push_back(p);
-        }
+        std::vector<int32_t> ids(n);
+        check(ikdg_acquire_removed_points(t_, nullptr, ids.data(), n, &n), "acquire_removed_points");
+        for (int64_t i = 0; i < n; ++i) removed_points.push_back(payload(ids[i]));
+        compact();
     }
+
+    // Points held by the host-side payload store (live ones plus garbage not
+    // yet dropped); at most about twice the points the tree can still return.
+    size_t stored_payloads() const { return pay_.size(); }
 
     // Public members of the reference kept for source compatibility
     // (ikd_Tree.h:246-248).  Root_Node is non-null exactly while the tree
@@ -292,7 +303,51 @@ class KD_TREE {
 
     ikdg_tree* t_ = nullptr;
     char root_token_ = 0;
-    std::vector<PointType> store_;  // inserted points by id
+    // Payload store: ids_ ascending (ids are handed out in increasing order)
+    // with the inserted point of each id at the same position in pay_.
+    std::vector<int32_t> ids_;
+    std::vector<PointType> pay_;
+    int64_t next_id_ = 0;
+
+    template <class V>
+    void remember(const V& pts) {
+        ids_.reserve(ids_.size() + pts.size());
+        pay_.reserve(pay_.size() + pts.size());
+        for (size_t i = 0; i < pts.size(); ++i) {
+            ids_.push_back((int32_t)(next_id_ + (int64_t)i));
+            pay_.push_back(pts[i]);
+        }
+        next_id_ += (int64_t)pts.size();
+    }
+    const PointType& payload(int32_t id) const {
+        auto it = std::lower_bound(ids_.begin(), ids_.end(), id);
+        if (it == ids_.end() || *it != id) throw IkdgError(IKDG_INTERNAL, "ikdg: no stored point for a returned id");
+        return pay_[it - ids_.begin()];
+    }
+    // Drops the payloads of ids the tree can no longer return, once they
+    // outnumber the live ones.
+    void compact() {
+        int64_t live = 0;
+        int st = ikdg_live_ids(t_, nullptr, 0, &live);
+        if (st != IKDG_OK && st != IKDG_CAPACITY) check(st, "live_ids");
+        if ((int64_t)ids_.size() <= 2 * live + 4096) return;
+        std::vector<int32_t> keep(live);
+        if (live > 0) check(ikdg_live_ids(t_, keep.data(), live, &live), "live_ids");
+        std::sort(keep.begin(), keep.end());
+        size_t w = 0, k = 0;
+        for (size_t r = 0; r < ids_.size(); ++r) {
+            while (k < keep.size() && keep[k] < ids_[r]) ++k;
+            if (k < keep.size() && keep[k] == ids_[r]) {
+                ids_[w] = ids_[r];
+                pay_[w] = pay_[r];
+                ++w;
+            }
+        }
+        ids_.resize(w);
+        pay_.erase(pay_.begin() + w, pay_.end());
+        ids_.shrink_to_fit();
+        pay_.shrink_to_fit();
+    }
 
     void check(int st, const char* what) {
         if (st != IKDG_OK)
@@ -331,7 +386,7 @@ class KD_TREE {
         check(call(offs.data(), ids.data(), total, &total), "range search");
         for (size_t i = 0; i < nq; ++i) {
             results[i].reserve(offs[i + 1] - offs[i]);
-            for (int64_t j = offs[i]; j < offs[i + 1]; ++j) results[i].push_back(store_[ids[j]]);
+            for (int64_t j = offs[i]; j < offs[i + 1]; ++j) results[i].push_back(payload(ids[j]));
         }
     }
 };

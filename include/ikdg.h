@@ -242,9 +242,19 @@ int ikdg_root_alpha(ikdg_tree* t, float* alpha_bal, float* alpha_del);
 int ikdg_flatten(ikdg_tree* t, float* xyz, int32_t* ids, int64_t capacity, int64_t* n);
 
 /* acquire_removed_points (ikd_Tree.cpp:558-571): drains the points deleted by
- * box or point deletion that rebuilds have dropped since the last call.
- * IKDG_CAPACITY with *n = required size (nothing drained) when too small. */
-int ikdg_acquire_removed_points(ikdg_tree* t, float* xyz, int64_t capacity, int64_t* n);
+ * box or point deletion that rebuilds have dropped since the last call, with
+ * their ids (xyz or ids may be NULL, not both).  IKDG_CAPACITY with *n =
+ * required size (nothing drained) when too small. */
+int ikdg_acquire_removed_points(ikdg_tree* t, float* xyz, int32_t* ids, int64_t capacity, int64_t* n);
+
+/* Ids of every point the tree can still hand back (no counterpart in the
+ * reference, whose nodes carry the whole PointType): the stored points, valid
+ * or deleted but not yet dropped by a rebuild (Add_Point_Boxes can restore
+ * those), followed by the removed points ikdg_acquire_removed_points has not
+ * drained yet.  Bindings that keep per-point payloads on the host, keyed by
+ * id, use it to drop payloads no search can return any more.  IKDG_CAPACITY
+ * with *n = required size when ids is NULL or capacity is too small. */
+int ikdg_live_ids(ikdg_tree* t, int32_t* ids, int64_t capacity, int64_t* n);
 
 /* Rebuilds the whole tree from its valid points (compaction). */
 int ikdg_rebuild(ikdg_tree* t);

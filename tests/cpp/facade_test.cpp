@@ -132,6 +132,90 @@ int main() {
     CHECK(ab >= 0.5f && ab <= 1.f && ad >= 0.f && ad <= 1.f);
     BoxPointType r = tree->tree_range();
     CHECK(r.vertex_min[0] >= -10 && r.vertex_max[0] <= 10);
+
+    // acquire_removed_points hands back the removed points as inserted,
+    // payload included.  delete_param 0: every subtree holding a deleted
+    // point is rebuilt, so every deleted point is dropped and recorded.
+    {
+        Tree t2(0.0, 0.6, 0.2);
+        PV c2(3000);
+        for (size_t i = 0; i < c2.size(); ++i) {
+            c2[i].x = U(rng);
+            c2[i].y = U(rng);
+            c2[i].z = U(rng);
+            c2[i].intensity = (float)i;
+        }
+        t2.Build(c2);
+        PV gone(c2.begin() + 10, c2.begin() + 60);
+        t2.Delete_Points(gone);
+        std::vector<BoxPointType> b2(1, box);
+        int nb = t2.Delete_Point_Boxes(b2);
+        PV removed;
+        t2.acquire_removed_points(removed);
+        CHECK((int)removed.size() == 50 + nb);
+        int from_list = 0;
+        for (auto& p : removed) {
+            const int i = (int)p.intensity;
+            CHECK(i >= 0 && i < (int)c2.size());
+            CHECK(c2[i].x == p.x && c2[i].y == p.y && c2[i].z == p.z);
+            const bool in_box = p.x >= -2 && p.x < 3 && p.y >= -2 && p.y < 3 && p.z >= -2 && p.z < 3;
+            from_list += (i >= 10 && i < 60 && !in_box);
+            CHECK(in_box || (i >= 10 && i < 60));
+        }
+        CHECK(t2.validnum() == 3000 - (int)removed.size());
+        PV again;
+        t2.acquire_removed_points(again);
+        CHECK(again.empty());
+        (void)from_list;
+    }
+
+    // A long mapping stream keeps the host-side payload store bounded by the
+    // points the tree can still return (plus a fixed slack), not by the
+    // number of points ever inserted.
+    {
+        Tree t3(0.5, 0.6, 0.3);
+        PV seed(20000);
+        for (auto& p : seed) {
+            p.x = U(rng);
+            p.y = U(rng);
+            p.z = U(rng);
+        }
+        t3.Build(seed);
+        std::uniform_real_distribution<float> V(-1, 1);
+        size_t inserted = seed.size();
+        for (int it = 0; it < 60; ++it) {
+            const float cx = -8.f + 0.25f * (float)it;
+            PV scan(5000);
+            for (size_t i = 0; i < scan.size(); ++i) {
+                scan[i].x = cx + 2.f * V(rng);
+                scan[i].y = U(rng);
+                scan[i].z = U(rng);
+                scan[i].intensity = (float)(inserted + i);
+            }
+            inserted += scan.size();
+            t3.Add_Points(scan, true);
+            BoxPointType behind;
+            behind.vertex_min[0] = -100;
+            behind.vertex_max[0] = cx - 3.f;
+            for (int a = 1; a < 3; ++a) {
+                behind.vertex_min[a] = -100;
+                behind.vertex_max[a] = 100;
+            }
+            std::vector<BoxPointType> bb(1, behind);
+            t3.Delete_Point_Boxes(bb);
+            PV dropped;
+            t3.acquire_removed_points(dropped);
+            CHECK(t3.stored_payloads() <= 2 * (size_t)t3.size() + 4096);
+        }
+        CHECK(inserted > 2 * t3.stored_payloads());
+        PV nn;
+        std::vector<float> dist;
+        PointXYZI q;
+        q.x = 6.f;
+        t3.Nearest_Search(q, 5, nn, dist);
+        CHECK(nn.size() == 5);
+        for (auto& p : nn) CHECK(p.intensity >= 0.f);
+    }
     std::printf("facade ok: deleted %d, downsampled inserts %d, valid %d\n", deleted, n_ds, tree->validnum());
     return 0;
 }

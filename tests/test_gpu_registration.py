@@ -200,3 +200,75 @@ def test_autograd_function_descends(scene):
                 cur, cur_loss = cand, lc
                 break
     assert cur_loss < first
+
+
+def rotation_like_library(pose):
+    """R(omega) in the operation order of the library's host code (Rodrigues,
+    [w]x^2 by explicit sums), so the transformed points round the same way."""
+    w = [float(v) for v in pose[:3]]
+    th = math.sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2])
+    if th < 1e-6:
+        a, b = 1.0 - th * th / 6.0, 0.5 - th * th / 24.0
+    else:
+        a, b = math.sin(th) / th, (1.0 - math.cos(th)) / (th * th)
+    Kx = [0.0, -w[2], w[1], w[2], 0.0, -w[0], -w[1], w[0], 0.0]
+    K2 = [0.0] * 9
+    for r in range(3):
+        for c in range(3):
+            s = 0.0
+            for m in range(3):
+                s += Kx[3 * r + m] * Kx[3 * m + c]
+            K2[3 * r + c] = s
+    return [(1.0 if i % 4 == 0 else 0.0) + a * Kx[i] + b * K2[i] for i in range(9)]
+
+
+def test_plane_fit_and_residuals_match_fp64(scene, ikdg_mod):
+    """The forward pass pinned independently of the GPU's own planes: every
+    scan point is transformed as the kernel does, its k = 5 neighbours come
+    from the oracle port, and an FP64 least-squares fit (QR, the way
+    FAST-LIO2's Eigen solve does it) gives the plane, the validity (every
+    neighbour within the threshold) and the residual, which the GPU's
+    planes, flags and residuals must match."""
+    import oracle_lib
+    tree, p, pose = scene
+    dev = torch.device("cuda", 0)
+    n = len(p)
+    pts = torch.from_numpy(p).to(dev)
+    planes = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    res = torch.empty((n,), dtype=torch.float32, device=dev)
+    valid = torch.empty((n,), dtype=torch.int32, device=dev)
+    tree.p2p_forward(pts.data_ptr(), n, pose, K, MAX_DIST, THRESH, planes.data_ptr(), res.data_ptr(),
+                     valid.data_ptr())
+    tree.synchronize()
+    P = planes.cpu().numpy().astype(np.float64)
+    V = valid.cpu().numpy().astype(bool)
+    R = rotation_like_library(pose)
+    p64 = p.astype(np.float64)
+    w64 = np.stack([((R[3 * r] * p64[:, 0] + R[3 * r + 1] * p64[:, 1]) + R[3 * r + 2] * p64[:, 2]) + pose[3 + r]
+                    for r in range(3)], 1)
+    w32 = w64.astype(np.float32)
+    if not oracle_lib.available("port"):
+        oracle_lib.build("port")
+    cpu = oracle_lib.OracleTree(0.5, 0.6, 0.5, kind="port")
+    cpu.Build(tree.flatten())
+    nb, _, cnt = cpu.knn(w32, K, MAX_DIST, nthreads=8)
+    cpu.close()
+    full = cnt == K
+    assert not V[~full].any(), "a point with fewer than k neighbours was marked valid"
+    A = nb[full].astype(np.float64)                              # [m, k, 3]
+    Q, Rm = np.linalg.qr(A)
+    x = np.linalg.solve(Rm, (Q.transpose(0, 2, 1) @ -np.ones((len(A), K, 1))))[..., 0]
+    norm = np.linalg.norm(x, axis=1)
+    n64, d64 = x / norm[:, None], 1.0 / norm
+    e = np.abs((A * n64[:, None, :]).sum(2) + d64[:, None])       # [m, k]
+    valid64 = (e <= THRESH).all(1)
+    border = (np.abs(e - THRESH) < 1e-5).any(1)
+    Vf = V[full]
+    assert np.array_equal(Vf[~border], valid64[~border]), "validity differs from the FP64 fit"
+    ok = valid64 & Vf
+    assert ok.sum() > 0.5 * n
+    assert np.abs(P[full][ok, 0:3] - n64[ok]).max() < 1e-5, "plane normals differ"
+    assert (np.abs(P[full][ok, 3] - d64[ok]) <= 1e-5 * np.maximum(1.0, np.abs(d64[ok]))).all(), "offsets differ"
+    r64 = (n64 * w64[full]).sum(1) + d64
+    r_gpu = res.cpu().numpy().astype(np.float64)[full]
+    assert np.abs(r_gpu[ok] - r64[ok]).max() < 2e-4, "residuals differ from the FP64 fit"
