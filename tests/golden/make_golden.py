@@ -156,18 +156,18 @@ def restore_fixture():
 
     Both phases are laid out so that the reference's result does not depend on
     its tree shape:
-    * phase A (delete_param 0.5): sparse point deletions, thin slab deletions
-      and a downsampled insertion that downsample-deletes about half of 300
-      stored points; nothing is dense enough to trigger a rebuild (size()
-      stays the number of stored points), so every deleted point is still
-      stored when one box covering all space restores them.  Points removed
-      by downsampling stay deleted.
+    * phase A (delete_param 0.5): a downsampled insertion that
+      downsample-deletes about half of 300 stored points, then sparse point
+      deletions and thin slab deletions; nothing is dense enough to trigger a
+      rebuild (size() stays the number of stored points), so every deleted
+      point is still stored when one box covering all space restores them.
+      Points removed by downsampling stay deleted.
     * phase B (delete_param 0, a tree of 1,400 points, so that every rebuild
       runs inline): every subtree that holds a deleted point violates the
       delete criterion, so rebuilds purge every deleted point and
       acquire_removed_points returns all point- and box-deleted ones (not the
       downsample-deleted ones)."""
-    rng = np.random.default_rng(15)
+    rng = np.random.default_rng(16)  # a seed whose phase A runs no rebuild in the reference
     L = 50.0
     base = rng.uniform(-L, L, (100000, 3)).astype(F32)
     out = {"base": base}
@@ -177,15 +177,18 @@ def restore_fixture():
     # (root_alpha right after Build is not recorded: BuildTree never sets the
     # root's alpha fields, ikd_Tree.cpp:573-622, so they hold whatever the
     # allocation held)
+    # the downsampled insertion comes first: with no deleted point in the
+    # tree yet, the reference's lazy subtree flags cannot carry the
+    # downsample mark onto points deleted earlier (which depends on its shape)
+    near = base[rng.choice(len(base), 300, replace=False)] + F32(0.001)
+    out["a_dsadd"] = near.astype(F32)
+    out["a_dsadd_ret"] = np.int64(t.Add_Points(near.astype(F32), True))
     dp = base[rng.choice(len(base), 1500, replace=False)]
     t.Delete_Points(dp)
     xs = rng.uniform(-L, L, 4)
     slabs = np.array([[x, -100, -100, x + 0.3, 100, 100] for x in xs], F32)
     out["a_delpts"], out["a_slabs"] = dp, slabs
     out["a_slab_ret"] = np.int64(t.Delete_Point_Boxes(slabs))
-    near = base[rng.choice(len(base), 300, replace=False)] + F32(0.001)
-    out["a_dsadd"] = near.astype(F32)
-    out["a_dsadd_ret"] = np.int64(t.Add_Points(near.astype(F32), True))
     out["a_size"] = np.int64(t.size())
     out["a_validnum"] = np.int64(t.validnum())
     out["a_range"] = t.tree_range()

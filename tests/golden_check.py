@@ -220,9 +220,9 @@ def replay_restore_fixture(make_tree):
     t = make_tree(0.5, 0.6, 0.2)
     t.Build(g["base"])
     assert np.array_equal(bits(t.tree_range()), bits(g["a_range_built"])), "tree_range after Build"
+    assert t.Add_Points(g["a_dsadd"], True) == int(g["a_dsadd_ret"]), "downsampled insert count"
     t.Delete_Points(g["a_delpts"])
     assert t.Delete_Point_Boxes(g["a_slabs"]) == int(g["a_slab_ret"]), "slab deletion count"
-    assert t.Add_Points(g["a_dsadd"], True) == int(g["a_dsadd_ret"]), "downsampled insert count"
     assert t.size() == int(g["a_size"]), "size(): a rebuild ran where the reference ran none"
     assert t.validnum() == int(g["a_validnum"])
     assert np.array_equal(bits(t.tree_range()), bits(g["a_range"])), "tree_range after deletions"
