@@ -424,6 +424,12 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
 
     plain_ms = timed(plain)
     plain_sync_ms = timed(plain_sync)
+    b.set_query_order(False)
+    batch_unordered_ms = timed(batched)
+    b.set_query_order(True)
+    b.set_range_staging(False)
+    batch_two_pass_ms = timed(batched)
+    b.set_range_staging(True)
     batch_ms = timed(batched)
     batch_dev = batch_device_ms()
     tuned = None
@@ -450,6 +456,12 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
         "plain_sync": "the same calls, each awaited before the next",
         "batched_ms": batch_ms, "batched_queries_per_s": n_queries / (batch_ms / 1e3),
         "batched_device_ms": batch_dev,
+        "batched_unordered_ms": batch_unordered_ms,
+        "batched_unordered": "the same batch with every request's queries searched in the given order "
+                             "(query ordering off)",
+        "batched_two_pass_ms": batch_two_pass_ms,
+        "batched_two_pass": "the same batch with range requests as a counting walk plus a writing walk "
+                            "(single pass off)",
         "speedup_vs_plain": plain_ms / batch_ms,
         "speedup_vs_plain_sync": plain_sync_ms / batch_ms,
         "autotuned": tuned,

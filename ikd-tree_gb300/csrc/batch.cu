@@ -69,34 +69,137 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
             const int g = threadIdx.x / G;
             const long long tid = (c - R.c1) * (BATCH_CHUNK / G) + lane / G;
             search::knn_body<0, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
-                                   nullptr, sd + g, si + g, ss + g, groups);
+                                   R.perm, sd + g, si + g, ss + g, groups);
         } else if constexpr (KC < BATCH_RANGE_CLASS) {
             const long long tid = (c - R.c1) * (BATCH_CHUNK / G) + lane / G;
             search::knn_body<KM, G>(t, tid, R.q, R.q_stride, R.nq, R.k, R.max_sq, R.ids, R.d2, R.xyz, R.cnt, nullptr,
-                                    nullptr);
+                                    R.perm);
         } else {
             // warp-collective body: every lane calls it
-            const long long qi = (c - R.c1) * BATCH_CHUNK + lane;
+            long long qi = (c - R.c1) * BATCH_CHUNK + lane;
             const bool valid = qi < R.nq;
+            if (valid && R.perm != nullptr) qi = __ldg(R.perm + qi);
             const long long n =
                 R.kind == BATCH_BOX
-                    ? search::range_body<0, false>(t, R.q, R.q_stride, nullptr, 0, qi, valid, 0, 0, nullptr, nullptr)
-                    : search::range_body<1, false>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, valid, 0, 0,
+                    ? search::range_body<0, search::RANGE_COUNT>(t, R.q, R.q_stride, nullptr, 0, qi, valid, 0, 0,
+                                                                 nullptr, nullptr)
+                    : search::range_body<1, search::RANGE_COUNT>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, valid,
+                                                                 0, 0,
                                                    nullptr, nullptr);
             if (valid) counts[R.cbase + qi] = n;
         }
     }
 }
 
-// Phase 2: range requests write their CSR offsets and, where the request's
-// capacity holds the query's results, the ids / points.
+// Phase 1 of the range requests, single pass: every query walked once in
+// write mode, its hits staged (search.cuh RangeStage) and its hit count stored
+// in counts[cbase + qi].
+__global__ void __launch_bounds__(BATCH_THREADS) batch_range_stage_kernel(const DevTree* __restrict__ trees,
+                                                                          const BatchReq* __restrict__ reqs,
+                                                                          const long long* __restrict__ req_c1,
+                                                                          int r0, int r1, long long c_begin,
+                                                                          long long c_end,
+                                                                          long long* __restrict__ counts,
+                                                                          unsigned long long* __restrict__ ctr,
+                                                                          search::RangeStage st) {
+    const int lane = threadIdx.x & 31;
+    search::StageCursor cur;
+    for (;;) {
+        long long c = 0;
+        int r = -1;
+        if (lane == 0) {
+            c = c_begin + (long long)atomicAdd(ctr, 1ull);
+            r = c < c_end ? find_req(req_c1, r0, r1, c) : -1;
+        }
+        c = __shfl_sync(0xffffffffu, c, 0);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (c >= c_end) break;
+        const BatchReq& R = reqs[r];
+        const DevTree t = trees[R.tree];
+        long long qi = (c - R.c1) * BATCH_CHUNK + lane;
+        const bool valid = qi < R.nq;
+        if (valid && R.perm != nullptr) qi = __ldg(R.perm + qi);
+        search::RangeStage rs = st;
+        rs.qbase = (int)R.cbase;
+        const long long n =
+            R.kind == BATCH_BOX
+                ? search::range_body<0, search::RANGE_STAGE>(t, R.q, R.q_stride, nullptr, 0, qi, valid, 0, 0, nullptr,
+                                                             nullptr, &rs, &cur)
+                : search::range_body<1, search::RANGE_STAGE>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, valid, 0,
+                                                             0, nullptr, nullptr, &rs, &cur);
+        if (valid) counts[R.cbase + qi] = n;
+    }
+    if (lane == 0) search::stage_close(st, cur);
+}
+
+// After the count scan: each range query's CSR offset (and each request's
+// total); a query whose results would end past its request's capacity raises
+// ERR_OUTPUT (its hits are not copied).  rq_base: batch-global first query of
+// every range request, ascending; rq_req: the request.
+__global__ void batch_offsets_kernel(const DevTree* __restrict__ trees, const BatchReq* __restrict__ reqs,
+                                     const long long* __restrict__ rq_base, const int* __restrict__ rq_req, int nr,
+                                     long long n_range, const long long* __restrict__ goff) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_range) return;
+    const int j = find_req(rq_base, 0, nr, g);
+    const BatchReq& R = reqs[rq_req[j]];
+    const long long qi = g - R.cbase;
+    const long long base = goff[R.cbase];
+    const long long o = goff[g] - base, e = goff[g + 1] - base;
+    R.offsets[qi] = o;
+    if (qi == R.nq - 1) {
+        R.offsets[R.nq] = e;
+        if (R.total != nullptr) *R.total = e;
+    }
+    if (e > o && R.ids != nullptr && e > R.capacity) atomicOr(&trees[R.tree].st->err, ERR_OUTPUT);
+}
+
+// Moves the staged hits to their CSR places: one warp per run record.
+__global__ void __launch_bounds__(BATCH_THREADS) batch_copy_kernel(const BatchReq* __restrict__ reqs,
+                                                                   const long long* __restrict__ rq_base,
+                                                                   const int* __restrict__ rq_req, int nr,
+                                                                   const long long* __restrict__ goff,
+                                                                   search::RangeStage st) {
+    if (*st.overflow) return;  // the direct write pass rewrites every range request
+    const int lane = threadIdx.x & 31;
+    const long long nruns = min((long long)*st.run_ctr, st.run_cap);
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = w0; w < nruns; w += nw) {
+        const int4 run = st.runs[w];
+        if (run.z <= 0) continue;
+        const long long g = run.x;
+        const int j = find_req(rq_base, 0, nr, g);
+        const BatchReq& R = reqs[rq_req[j]];
+        if (R.ids == nullptr) continue;
+        const long long base = goff[R.cbase];
+        if (goff[g + 1] - base > R.capacity) continue;
+        if (lane < run.z) {
+            const float4 h = st.hits[(long long)run.y + lane];
+            const long long d = goff[g] - base + run.w + lane;
+            R.ids[d] = (int)__float_as_uint(h.w);
+            if (R.xyz != nullptr) {
+                R.xyz[3 * d] = h.x;
+                R.xyz[3 * d + 1] = h.y;
+                R.xyz[3 * d + 2] = h.z;
+            }
+        }
+    }
+}
+
+// Phase 2 (two-pass form, and the single pass's fallback when its staging
+// overflowed; with only_if set it runs only when *only_if != 0): range
+// requests write their CSR offsets and, where the request's capacity holds
+// the query's results, the ids / points.
 __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTree* __restrict__ trees,
                                                                     const BatchReq* __restrict__ reqs,
                                                                     const int* __restrict__ ridx,
                                                                     const long long* __restrict__ req_c2, int nr,
                                                                     long long c_end,
                                                                     const long long* __restrict__ goff,
-                                                                    unsigned long long* __restrict__ ctr) {
+                                                                    unsigned long long* __restrict__ ctr,
+                                                                    const int* __restrict__ only_if) {
+    if (only_if != nullptr && *only_if == 0) return;
     const int lane = threadIdx.x & 31;
     for (;;) {
         long long c = 0;
@@ -110,15 +213,16 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTre
         if (c >= c_end) break;
         const BatchReq& R = reqs[r];
         const DevTree t = trees[R.tree];
-        const long long qi = (c - R.c2) * BATCH_CHUNK + lane;
+        const long long pos = (c - R.c2) * BATCH_CHUNK + lane;
+        const long long qi = pos < R.nq && R.perm != nullptr ? (long long)__ldg(R.perm + pos) : pos;
         const long long base = goff[R.cbase];
-        if (qi == 0) {
+        if (pos == 0) {
             const long long tot = goff[R.cbase + R.nq] - base;
             R.offsets[R.nq] = tot;
             if (R.total != nullptr) *R.total = tot;
         }
         // warp-collective body: every lane calls it, lanes without work idle
-        bool go = qi < R.nq;
+        bool go = pos < R.nq;
         long long o = 0, n = 0;
         if (go) {
             o = goff[R.cbase + qi] - base;
@@ -132,10 +236,47 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTre
             }
         }
         if (R.kind == BATCH_BOX)
-            search::range_body<0, true>(t, R.q, R.q_stride, nullptr, 0, qi, go, o, o + n, R.ids, R.xyz);
+            search::range_body<0, search::RANGE_WRITE>(t, R.q, R.q_stride, nullptr, 0, qi, go, o, o + n, R.ids,
+                                                       R.xyz);
         else
-            search::range_body<1, true>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, go, o, o + n, R.ids, R.xyz);
+            search::range_body<1, search::RANGE_WRITE>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, go, o, o + n,
+                                                       R.ids, R.xyz);
     }
+}
+
+// Every third bit of a 10-bit value (Morton interleave).
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void batch_key_kernel(const DevTree* __restrict__ trees, const BatchReq* __restrict__ reqs,
+                                 const long long* __restrict__ qstart, int n, long long total, int req_bits,
+                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int p = find_req(qstart, 0, n, g);
+    const BatchReq& R = reqs[p];
+    const long long qi = g - qstart[p];
+    float c[3];
+    const float* q = R.q + qi * R.q_stride;
+    for (int a = 0; a < 3; ++a) c[a] = R.kind == BATCH_BOX ? 0.5f * (q[a] + q[3 + a]) : q[a];
+    // the root's box is the left-child box of the sentinel record (node 0)
+    const float4 f0 = trees[R.tree].node[0], f1 = trees[R.tree].node[1];
+    const float lo[3] = {f0.x, f0.y, f0.z}, hi[3] = {f0.w, f1.x, f1.y};
+    uint32_t m = 0;
+    for (int a = 0; a < 3; ++a) {
+        const float t = (c[a] - lo[a]) / (hi[a] - lo[a]);
+        const int v = hi[a] > lo[a] && t > 0.f ? (t < 1.f ? (int)(t * 1024.f) : 1023) : 0;
+        m |= spread3((uint32_t)min(v, 1023)) << a;
+    }
+    const int mb = 32 - req_bits;  // Morton bits kept below the request position
+    keys[g] = ((uint32_t)p << mb) | (mb >= 30 ? m : m >> (30 - mb));
+    vals[g] = (uint32_t)qi;
 }
 
 std::mutex g_grid_mu;
@@ -219,6 +360,34 @@ int batch_write_grid() {
     return resident_grid((const void*)batch_write_kernel);
 }
 
+int batch_stage_grid() {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    return resident_grid((const void*)batch_range_stage_kernel);
+}
+
+void launch_batch_range_stage(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
+                              long long c_begin, long long c_end, long long* counts, unsigned long long* ctr,
+                              const search::RangeStage& st, int grid, cudaStream_t s) {
+    if (c_end <= c_begin || r1 <= r0) return;
+    const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
+    batch_range_stage_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr,
+                                                         st);
+}
+
+void launch_batch_offsets(const DevTree* trees, const BatchReq* reqs, const long long* rq_base, const int* rq_req,
+                          int nr, long long n_range, const long long* goff, cudaStream_t s) {
+    if (n_range <= 0 || nr <= 0) return;
+    batch_offsets_kernel<<<(unsigned)((n_range + 255) / 256), 256, 0, s>>>(trees, reqs, rq_base, rq_req, nr, n_range,
+                                                                           goff);
+}
+
+void launch_batch_copy(const BatchReq* reqs, const long long* rq_base, const int* rq_req, int nr,
+                       const long long* goff, const search::RangeStage& st, int grid, cudaStream_t s) {
+    if (nr <= 0) return;
+    batch_copy_kernel<<<grid, BATCH_THREADS, 0, s>>>(reqs, rq_base, rq_req, nr, goff, st);
+}
+
 void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
                          long long c_begin, long long c_end, int kclass, int lanes, long long* counts,
                          unsigned long long* ctr, int grid, cudaStream_t s) {
@@ -228,12 +397,20 @@ void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long 
     search_dispatch(kclass, lanes, true, nullptr, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
 }
 
+void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long long* qstart, int n, long long total,
+                       int req_bits, uint32_t* keys, uint32_t* vals, cudaStream_t s) {
+    if (total <= 0 || n <= 0) return;
+    batch_key_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(trees, reqs, qstart, n, total, req_bits, keys,
+                                                                      vals);
+}
+
 void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
-                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s) {
+                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s,
+                        const int* only_if) {
     if (c_end <= 0 || nr <= 0) return;
     const long long ctas = (c_end + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
     const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
-    batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr);
+    batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr, only_if);
 }
 
 }  // namespace ikdg

@@ -20,6 +20,7 @@
 
 #include "ikdg.h"
 #include "kernels.cuh"
+#include "search.cuh"
 #include "update.cuh"
 
 
@@ -1140,6 +1141,18 @@ struct Batch {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool use_graph = true;
+    // Run every request's queries in spatial order (Morton code in the tree's
+    // box): one key pass and one radix sort over the whole batch, then the
+    // search and write kernels take a request's queries through that order,
+    // so the lanes of a warp walk nearby nodes and leaves.  Results stay in
+    // query order.
+    bool use_order = true;
+    // Range requests in one pass: each query walked once with its hits staged
+    // in a batch-wide array, then copied to their CSR places once the counts
+    // are scanned (instead of a counting walk and a writing walk).  If the
+    // staging array overflows, the writing walk runs as before.
+    bool use_stage = true;
+    long long stage_hits = 0;  // staging slots (0: the requests' capacities plus per-warp slack)
     std::vector<Req> reqs;  // in the order added
     std::mutex mu;
     std::string err;
@@ -1163,6 +1176,20 @@ struct Batch {
     long long* d_totals = nullptr;
     unsigned long long* d_ctr = nullptr;
     void* d_scan = nullptr;
+    // query order (use_order): per request first query, keys / values of the sort
+    long long n_queries = 0;
+    int req_bits = 0;
+    bool ordered = false;
+    long long* d_qstart = nullptr;
+    uint32_t* d_okeys[2] = {nullptr, nullptr};
+    uint32_t* d_ovals[2] = {nullptr, nullptr};
+    void* d_osort = nullptr;
+    // single-pass range requests (use_stage)
+    bool staged = false;
+    search::RangeStage stage{};
+    long long* d_rq_base = nullptr;
+    int* d_rq_req = nullptr;
+    int n_rq = 0, stage_grid = 0;
     DevStatus* d_st = nullptr;
     DevTree* h_trees = nullptr;      // pinned: read by the graph's first copy
     DevStatus* h_st = nullptr;       // pinned
@@ -1280,6 +1307,12 @@ struct Batch {
             c1[p] = b.c1;
         }
         n_range_queries = cbase;
+        std::vector<long long> qstart(n + 1, 0);
+        for (int p = 0; p < n; ++p) qstart[p + 1] = qstart[p] + d[p].nq;
+        n_queries = qstart[n];
+        req_bits = 1;
+        while ((1 << req_bits) < n) ++req_bits;
+        ordered = use_order && n_queries >= QBIN_MIN_QUERIES && req_bits <= 24;
         // phase 2: range requests by c2
         std::vector<int> ridx;
         std::vector<long long> c2;
@@ -1299,6 +1332,30 @@ struct Batch {
         c2_end = chunk2;
         for (auto& g : groups) g.grid = batch_search_grid(g.kclass, g.lanes);
         write_grid = batch_write_grid();
+        // range requests in ascending cbase (sorted order), for the offsets
+        // and copy kernels of the single pass
+        std::vector<long long> rq_base;
+        std::vector<int> rq_req;
+        long long cap_sum = 0;
+        for (int p = 0; p < n; ++p)
+            if (d[p].kind != BATCH_KNN) {
+                rq_base.push_back(d[p].cbase);
+                rq_req.push_back(p);
+                if (d[p].ids != nullptr) cap_sum += std::min<long long>(d[p].capacity, (long long)1 << 40);
+            }
+        n_rq = (int)rq_base.size();
+        staged = use_stage && n_range_queries > 0;
+        long long hit_cap = 0, run_cap = 0;
+        if (staged) {
+            stage_grid = batch_stage_grid();
+            const long long warps = (long long)stage_grid * (BATCH_THREADS / 32);
+            hit_cap = std::min<long long>(cap_sum, (long long)1 << 28) + warps * search::STAGE_HIT_SEG;
+            run_cap = hit_cap / 2 + warps * search::STAGE_RUN_SEG;
+            if (stage_hits > 0) {
+                hit_cap = std::min<long long>(stage_hits, (long long)1 << 30);
+                run_cap = hit_cap / 2 + 1;
+            }
+        }
         // one allocation for the plan
         const size_t nt = trees.size(), nr = range_reqs.size();
         size_t bytes = align_up(sizeof(DevTree) * nt) + align_up(sizeof(BatchReq) * n) +
@@ -1306,6 +1363,12 @@ struct Batch {
                        align_up(sizeof(int) * (ridx.size() + 1)) + 2 * align_up(sizeof(long long) * (cbase + 1)) +
                        align_up(sizeof(long long) * (nr + 1)) + align_up(sizeof(unsigned long long) * 64) +
                        align_up(scan_temp_bytes(cbase + 1)) + align_up(sizeof(DevStatus)) + 4096;
+        const long long nqo = ordered ? n_queries : 0;
+        bytes += align_up(sizeof(long long) * (n + 1)) + 4 * align_up(sizeof(uint32_t) * std::max<long long>(nqo, 1)) +
+                 align_up(ordered ? sort_temp_bytes(nqo, 1) : 0);
+        bytes += align_up(sizeof(long long) * (n_rq + 1)) + align_up(sizeof(int) * (n_rq + 1)) +
+                 align_up(sizeof(float4) * std::max<long long>(hit_cap, 1)) +
+                 align_up(sizeof(int4) * std::max<long long>(run_cap, 1)) + align_up(sizeof(unsigned long long) * 4);
         CK(cudaMalloc(&dev, bytes));
         Carver c(dev);
         d_trees = c.take<DevTree>(nt);
@@ -1319,10 +1382,33 @@ struct Batch {
         d_ctr = c.take<unsigned long long>(64);
         d_scan = c.take<char>(scan_temp_bytes(cbase + 1));
         d_st = c.take<DevStatus>(1);
+        d_qstart = c.take<long long>(n + 1);
+        for (int b2 = 0; b2 < 2; ++b2) {
+            d_okeys[b2] = c.take<uint32_t>(std::max<long long>(nqo, 1));
+            d_ovals[b2] = c.take<uint32_t>(std::max<long long>(nqo, 1));
+        }
+        d_osort = ordered ? (void*)c.take<char>(sort_temp_bytes(nqo, 1)) : nullptr;
+        for (int p = 0; p < n; ++p) d[p].perm = ordered ? (const int*)(d_ovals[0] + qstart[p]) : nullptr;
+        d_rq_base = c.take<long long>(n_rq + 1);
+        d_rq_req = c.take<int>(n_rq + 1);
+        stage.hits = c.take<float4>(std::max<long long>(hit_cap, 1));
+        stage.runs = c.take<int4>(std::max<long long>(run_cap, 1));
+        unsigned long long* sctr = c.take<unsigned long long>(4);
+        stage.hit_ctr = sctr;
+        stage.run_ctr = sctr + 1;
+        stage.overflow = (int*)(sctr + 2);
+        stage.hit_cap = hit_cap;
+        stage.run_cap = run_cap;
+        stage.qbase = 0;
         for (size_t j = 0; j < nr; ++j) d[pos_of[range_reqs[j]]].total = d_totals + j;
         CK(cudaMallocHost(&h_trees, sizeof(DevTree) * std::max<size_t>(nt, 1)));
         CK(cudaMemcpyAsync(d_reqs, d.data(), sizeof(BatchReq) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(d_c1, c1.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d_qstart, qstart.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
+        if (n_rq > 0) {
+            CK(cudaMemcpyAsync(d_rq_base, rq_base.data(), sizeof(long long) * n_rq, cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(d_rq_req, rq_req.data(), sizeof(int) * n_rq, cudaMemcpyHostToDevice, stream));
+        }
         if (!ridx.empty()) {
             CK(cudaMemcpyAsync(d_c2, c2.data(), sizeof(long long) * c2.size(), cudaMemcpyHostToDevice, stream));
             CK(cudaMemcpyAsync(d_ridx, ridx.data(), sizeof(int) * ridx.size(), cudaMemcpyHostToDevice, stream));
@@ -1370,19 +1456,38 @@ struct Batch {
         CK(cudaMemcpyAsync(d_trees, h_trees, sizeof(DevTree) * trees.size(), cudaMemcpyHostToDevice, stream));
         CK(cudaMemsetAsync(d_ctr, 0, sizeof(unsigned long long) * 64, stream));
         CK(cudaMemsetAsync(d_st, 0, sizeof(DevStatus), stream));
+        if (staged) CK(cudaMemsetAsync(stage.hit_ctr, 0, sizeof(unsigned long long) * 3, stream));
+        if (ordered) {
+            launch_batch_keys(d_trees, d_reqs, d_qstart, (int)reqs.size(), n_queries, req_bits, d_okeys[0],
+                              d_ovals[0], stream);
+            radix_sort_pairs(d_okeys[0], d_ovals[0], d_okeys[1], d_ovals[1], n_queries, 1, n_queries, 32, d_osort,
+                             stream);
+        }
         if (groups.size() > 1) CK(cudaEventRecord(ev_fork, stream));
         for (size_t g = 0; g < groups.size(); ++g) {
             const Group& G = groups[g];
             cudaStream_t s = g == 0 ? stream : branch[g - 1];
             if (g > 0) CK(cudaStreamWaitEvent(s, ev_fork, 0));
-            launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes, d_counts,
-                                d_ctr + g, G.grid, s);
+            if (staged && G.kclass == BATCH_RANGE_CLASS)
+                launch_batch_range_stage(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, d_counts, d_ctr + g,
+                                         stage, stage_grid, s);
+            else
+                launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes,
+                                    d_counts, d_ctr + g, G.grid, s);
             if (g > 0) CK(cudaEventRecord(ev_join[g - 1], s));
         }
         for (size_t g = 1; g < groups.size(); ++g) CK(cudaStreamWaitEvent(stream, ev_join[g - 1], 0));
         if (nridx > 0) {
             exclusive_scan(d_counts, d_goff, n_range_queries + 1, nullptr, d_scan, stream);
-            launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid, stream);
+            if (staged) {
+                launch_batch_offsets(d_trees, d_reqs, d_rq_base, d_rq_req, n_rq, n_range_queries, d_goff, stream);
+                launch_batch_copy(d_reqs, d_rq_base, d_rq_req, n_rq, d_goff, stage, write_grid, stream);
+                launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid,
+                                   stream, stage.overflow);
+            } else {
+                launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid,
+                                   stream);
+            }
         }
         // range requests without queries: empty CSR
         for (int j : range_reqs)
@@ -2027,6 +2132,22 @@ int ikdg_batch_set_graph(ikdg_batch* h, int use_graph) {
     return batch_guarded(h, [&](ikdg::Batch& b) {
         b.drop_plan();
         b.use_graph = use_graph != 0;
+    });
+}
+
+int ikdg_batch_set_query_order(ikdg_batch* h, int ordered) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        b.drop_plan();
+        b.use_order = ordered != 0;
+    });
+}
+
+int ikdg_batch_set_range_staging(ikdg_batch* h, int single_pass, int64_t hit_capacity) {
+    return batch_guarded(h, [&](ikdg::Batch& b) {
+        if (hit_capacity < 0) throw ikdg::BadArg{"batch: negative staging capacity"};
+        b.drop_plan();
+        b.use_stage = single_pass != 0;
+        b.stage_hits = hit_capacity;
     });
 }
 

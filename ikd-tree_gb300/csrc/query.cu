@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(128) range_kernel(DevTree t, const float* __re
     const bool valid = qi < nq;
     if (!WRITE) {
         const long long c =
-            search::range_body<MODE, false>(t, q, q_stride, radius, r_stride, qi, valid, 0, 0, nullptr, nullptr);
+            search::range_body<MODE, search::RANGE_COUNT>(t, q, q_stride, radius, r_stride, qi, valid, 0, 0, nullptr, nullptr);
         if (valid) counts[qi] = c;
         return;
     }
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) range_kernel(DevTree t, const float* __re
             go = false;
         }
     }
-    search::range_body<MODE, true>(t, q, q_stride, radius, r_stride, qi, go, o, o_lim, ids, xyz);
+    search::range_body<MODE, search::RANGE_WRITE>(t, q, q_stride, radius, r_stride, qi, go, o, o_lim, ids, xyz);
 }
 
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }

@@ -79,6 +79,8 @@ SIGNATURES = {
                                                _vp, C.c_int64, _ip]),
     "ikdg_batch_set_knn_lanes": (C.c_int, [_vp, C.c_int32, C.c_int32]),
     "ikdg_batch_set_graph": (C.c_int, [_vp, C.c_int]),
+    "ikdg_batch_set_query_order": (C.c_int, [_vp, C.c_int]),
+    "ikdg_batch_set_range_staging": (C.c_int, [_vp, C.c_int, C.c_int64]),
     "ikdg_batch_run": (C.c_int, [_vp]),
     "ikdg_batch_synchronize": (C.c_int, [_vp, _lp]),
     "ikdg_batch_autotune": (C.c_int, [_vp, C.c_int32, _ip]),
@@ -477,6 +479,16 @@ class Batch:
 
     def set_graph(self, use_graph: bool):
         self._check(self.lib.ikdg_batch_set_graph(self.h, 1 if use_graph else 0), "batch_set_graph")
+
+    def set_range_staging(self, single_pass: bool, hit_capacity: int = 0):
+        """Box / radius requests in one walk with staged hits (default), or a
+        counting walk and a writing walk."""
+        self._check(self.lib.ikdg_batch_set_range_staging(self.h, 1 if single_pass else 0, int(hit_capacity)),
+                    "batch_set_range_staging")
+
+    def set_query_order(self, ordered: bool):
+        """Search every request's queries in spatial (Morton) order (default on)."""
+        self._check(self.lib.ikdg_batch_set_query_order(self.h, 1 if ordered else 0), "batch_set_query_order")
 
     def run(self):
         self._check(self.lib.ikdg_batch_run(self.h), "batch_run")

@@ -4,10 +4,12 @@ Every request of a batch must give exactly what the same request gives
 through the per-call entry points (ikdg_knn_device, ikdg_box_search_device,
 ikdg_radius_search_device) on the same tree: kNN ids, squared distances,
 points and counts, and the box / radius CSR offsets, ids and points, bit for
-bit.  The per-call path itself is pinned to the oracle elsewhere; one request
-is also checked against the oracle here.  Covered: all kNN register classes
-and lanes values, an empty tree, trees mutated (pools grown) between runs of
-the same graph, runs without a graph, a capacity overflow, and the autotuner.
+bit.  The per-call path itself is pinned to the oracle elsewhere; a kNN, a
+box and a radius request are also checked against the numpy model here.
+Covered: all kNN register classes and lanes values, an empty tree, trees
+mutated (pools grown) between runs of the same graph, runs without a graph,
+queries in Morton order and in the given order, a capacity overflow, and the
+autotuner.
 """
 import math
 
@@ -212,6 +214,44 @@ def test_batch_knn_matches_oracle(scene):
     spec.Build(maps[0].points)
     sid, sd2 = spec.knn(maps[0].knn_q, r.k, r.max_dist)
     assert np.array_equal(ids, sid) and np.array_equal(d2.view(np.uint32), sd2.view(np.uint32))
+
+
+def test_batch_query_order_changes_nothing(scene):
+    """Searching every request's queries in Morton order (the default) and
+    in the given order gives the same bytes."""
+    maps, trees, empty, reqs, b = scene
+    ordered = batched(b, reqs)
+    b.set_query_order(False)
+    plain = batched(b, reqs)
+    b.set_query_order(True)
+    assert_same(ordered, plain, reqs)
+
+
+def test_batch_range_passes_agree(scene):
+    """Range requests in one walk with staged hits (the default), with a
+    staging array too small (the run falls back to the writing walk), and as
+    a counting walk plus a writing walk: the same bytes as the per-call path."""
+    maps, trees, empty, reqs, b = scene
+    ref = per_call(reqs)
+    for single, cap in ((True, 0), (True, 1000), (False, 0)):
+        b.set_range_staging(single, cap)
+        assert_same(batched(b, reqs), ref, reqs)
+    b.set_range_staging(True, 0)
+
+
+def test_batch_range_requests_match_oracle(scene):
+    """A box and a radius request of the batch against the numpy model: the
+    id set of every query."""
+    maps, trees, empty, reqs, b = scene
+    batched(b, reqs)
+    spec = SpecTree()
+    spec.Build(maps[0].points)
+    for r, want in ((reqs[1], spec.box_search(maps[0].boxes)),
+                    (reqs[2], spec.radius_search(maps[0].radius_q, maps[0].radius))):
+        off, ids, _ = r.outputs()
+        assert len(want) == len(off) - 1
+        for qi, w in enumerate(want):
+            assert np.array_equal(np.sort(ids[off[qi]:off[qi + 1]]), np.asarray(w)), f"{r.kind} query {qi}"
 
 
 def test_batch_after_mutation(ikdg_mod):
