@@ -16,6 +16,11 @@ using search::FINF;
 #define IKDG_KNN_THREADS 128
 #endif
 constexpr int KNN_THREADS = IKDG_KNN_THREADS;
+// 1: kNN rows of k <= 8 leave a warp through shared memory as coalesced spans
+#ifndef IKDG_KNN_STAGED_OUT
+#define IKDG_KNN_STAGED_OUT 1
+#endif
+constexpr bool KNN_STAGED_OUT = IKDG_KNN_STAGED_OUT != 0;
 
 template <int KMAX, int G>
 __global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
@@ -24,8 +29,15 @@ __global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float
                                                   int* __restrict__ out_cnt, int* __restrict__ slots,
                                                   const int* __restrict__ perm) {
     const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    search::knn_body<KMAX, G>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots,
-                              perm);
+    if constexpr (KMAX > 0 && G == 1 && KNN_STAGED_OUT) {
+        // rows of a warp's consecutive queries leave through shared memory
+        __shared__ __align__(16) float stage[KNN_THREADS / 32][search::knn_stage_floats(KMAX)];
+        search::knn_body<KMAX, G>(t, gtid, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm,
+                                  nullptr, nullptr, nullptr, 1, perm == nullptr ? stage[threadIdx.x >> 5] : nullptr);
+    } else {
+        search::knn_body<KMAX, G>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots,
+                                  perm);
+    }
 }
 
 // WRITE = false stores counts[qi]; true emits at [offsets[qi],

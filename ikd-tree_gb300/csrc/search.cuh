@@ -42,6 +42,27 @@ constexpr int RANGE_LEAF_BATCH = IKDG_RANGE_LEAF_BATCH;
 #define IKDG_KNN_LEAF_T 32
 #endif
 constexpr int KNN_LEAF_T = IKDG_KNN_LEAF_T;
+#ifndef IKDG_KNN_KEY64
+#define IKDG_KNN_KEY64 0
+#endif
+
+// Stores n floats (or int bits) from shared memory to dst with the whole warp:
+// 16-byte stores where dst is 16-byte aligned, lane-consecutive 4-byte stores
+// otherwise.  src is 16-byte aligned shared memory.
+__device__ __forceinline__ void warp_store(float* dst, const float* src, int n) {
+    const int lane = threadIdx.x & 31;
+    int done = 0;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        const int n4 = n >> 2;
+        for (int i = lane; i < n4; i += 32)
+            reinterpret_cast<float4*>(dst)[i] = reinterpret_cast<const float4*>(src)[i];
+        done = n4 << 2;
+    }
+    for (int i = done + lane; i < n; i += 32) dst[i] = src[i];
+}
+
+// Shared-memory floats per warp for the staged kNN output (k <= kmax).
+__host__ __device__ constexpr int knn_stage_floats(int kmax) { return 32 * (5 * kmax + 1); }
 
 __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
     return d < d2 || (d == d2 && id < id2);
@@ -69,7 +90,7 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                                          float* __restrict__ out_d2, float* __restrict__ out_xyz,
                                          int* __restrict__ out_cnt, int* __restrict__ slots,
                                          const int* __restrict__ perm, float* kd = nullptr, int* ki = nullptr,
-                                         int* ks = nullptr, int kst = 1) {
+                                         int* ks = nullptr, int kst = 1, float* wstage = nullptr) {
     const int sub = threadIdx.x & (G - 1);
     const int lane = threadIdx.x & 31;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
@@ -81,6 +102,15 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     const float qz = valid ? q[qi * q_stride + 2] : 0.f;
 
     constexpr int KR = KMAX > 0 ? KMAX : 1;
+#if IKDG_KNN_KEY64
+    unsigned long long bkey[KR];
+    int bsl[KR];
+#pragma unroll
+    for (int j = 0; j < KR; ++j) {
+        bkey[j] = 0x7f8000007fffffffull;  // (+inf, largest id)
+        bsl[j] = -1;
+    }
+#else
     float bd[KR];
     int bi[KR], bsl[KR];
 #pragma unroll
@@ -89,6 +119,7 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         bi[j] = 0x7fffffff;
         bsl[j] = -1;
     }
+#endif
     const bool in_rows = kd == nullptr;
     float* gd = in_rows ? out_d2 + qi * k : kd;
     int* gi = in_rows ? out_id + qi * k : ki;
@@ -145,6 +176,28 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
             }
             return;
         }
+#if IKDG_KNN_KEY64
+        // (distance, id) as one 64-bit key: distances are >= 0, so their bit
+        // patterns order like the floats and the id breaks ties.
+        unsigned long long ck = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
+        int cs = sl;
+#pragma unroll
+        for (int m = 0; m < KR; ++m) {
+            const bool sw = ck < bkey[m];
+            const unsigned long long tk = bkey[m];
+            const int ts = bsl[m];
+            bkey[m] = sw ? ck : tk;
+            bsl[m] = sw ? cs : ts;
+            ck = sw ? tk : ck;
+            cs = sw ? ts : cs;
+        }
+#pragma unroll
+        for (int m = 0; m < KR; ++m)
+            if (m == k - 1) {
+                worst = __uint_as_float((unsigned)(bkey[m] >> 32));
+                worst_id = (int)(unsigned)bkey[m];
+            }
+#else
         float cd = d;
         int cid = id, cs = sl;
 #pragma unroll
@@ -165,6 +218,7 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 worst = bd[m];
                 worst_id = bi[m];
             }
+#endif
     };
 
     while (true) {
@@ -261,6 +315,54 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         }
         pop();
     }
+    if constexpr (KMAX > 0 && G == 1) {
+        if (wstage != nullptr) {
+            // The warp's 32 queries are consecutive (no permutation): their
+            // rows form one contiguous span of every output array.  Stage the
+            // rows in shared memory, then write each span with coalesced,
+            // 16-byte stores (the outputs may be host memory over the chip
+            // link, where scattered 4-byte stores are slow).
+            const long long q0 = tid - lane;
+            const int nrows = (int)min(32ll, nq - q0);
+            if (nrows <= 0) return;
+            float* s_id = wstage;
+            float* s_d2 = s_id + 32 * KMAX;
+            float* s_xyz = s_d2 + 32 * KMAX;
+            float* s_cnt = s_xyz + 96 * KMAX;
+            if (valid) {
+                int cnt = 0;
+#pragma unroll
+                for (int j = 0; j < KR; ++j) {
+                    if (j < k) {
+                        const bool ok = bsl[j] >= 0;
+#if IKDG_KNN_KEY64
+                        const int id = ok ? (int)(unsigned)bkey[j] : -1;
+                        const float dd = ok ? __uint_as_float((unsigned)(bkey[j] >> 32)) : FINF;
+#else
+                        const int id = ok ? bi[j] : -1;
+                        const float dd = ok ? bd[j] : FINF;
+#endif
+                        s_id[lane * k + j] = __int_as_float(id);
+                        s_d2[lane * k + j] = dd;
+                        if (out_xyz != nullptr) {
+                            const float4 p = ok ? __ldg(P + bsl[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                            s_xyz[(lane * k + j) * 3 + 0] = p.x;
+                            s_xyz[(lane * k + j) * 3 + 1] = p.y;
+                            s_xyz[(lane * k + j) * 3 + 2] = p.z;
+                        }
+                        cnt += ok ? 1 : 0;
+                    }
+                }
+                s_cnt[lane] = __int_as_float(cnt);
+            }
+            __syncwarp();
+            warp_store(reinterpret_cast<float*>(out_id + q0 * k), s_id, nrows * k);
+            warp_store(out_d2 + q0 * k, s_d2, nrows * k);
+            if (out_xyz != nullptr) warp_store(out_xyz + q0 * k * 3, s_xyz, nrows * k * 3);
+            if (out_cnt != nullptr) warp_store(reinterpret_cast<float*>(out_cnt + q0), s_cnt, nrows);
+            return;
+        }
+    }
     if (!valid || sub != 0) return;
 
     if (KMAX == 0) {
@@ -284,8 +386,13 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     for (int j = 0; j < KR; ++j) {
         if (j < k) {
             const bool ok = bsl[j] >= 0;
+#if IKDG_KNN_KEY64
+            out_id[qi * k + j] = ok ? (int)(unsigned)bkey[j] : -1;
+            out_d2[qi * k + j] = ok ? __uint_as_float((unsigned)(bkey[j] >> 32)) : FINF;
+#else
             out_id[qi * k + j] = ok ? bi[j] : -1;
             out_d2[qi * k + j] = ok ? bd[j] : FINF;
+#endif
             if (out_xyz != nullptr) {
                 float4 p = ok ? __ldg(P + bsl[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
                 out_xyz[(qi * k + j) * 3 + 0] = p.x;

@@ -267,8 +267,18 @@ def test_plane_fit_and_residuals_match_fp64(scene, ikdg_mod):
     assert np.array_equal(Vf[~border], valid64[~border]), "validity differs from the FP64 fit"
     ok = valid64 & Vf
     assert ok.sum() > 0.5 * n
-    assert np.abs(P[full][ok, 0:3] - n64[ok]).max() < 1e-5, "plane normals differ"
-    assert (np.abs(P[full][ok, 3] - d64[ok]) <= 1e-5 * np.maximum(1.0, np.abs(d64[ok]))).all(), "offsets differ"
+    # every plane the GPU accepts fits its neighbours within the threshold
+    Pf = P[full]
+    e_gpu = np.abs((A * Pf[:, None, 0:3]).sum(2) + Pf[:, 3:4])
+    assert (e_gpu[Vf] <= THRESH + 1e-5).all(), "an accepted plane misses a neighbour"
+    # The A x = -1 form of the fit is ill-conditioned for planes that pass
+    # near the origin (the ground z = 0 among them): there the normal is
+    # ill-defined and two exact solvers may differ.  Normals, offsets and
+    # residuals are compared where the fit is well conditioned.
+    well = ok & (np.linalg.cond(A) < 1e4)
+    assert well.sum() > 0.2 * ok.sum(), "too few well-conditioned planes to compare"
+    assert np.abs(Pf[well, 0:3] - n64[well]).max() < 1e-5, "plane normals differ"
+    assert (np.abs(Pf[well, 3] - d64[well]) <= 1e-5 * np.maximum(1.0, np.abs(d64[well]))).all(), "offsets differ"
     r64 = (n64 * w64[full]).sum(1) + d64
     r_gpu = res.cpu().numpy().astype(np.float64)[full]
-    assert np.abs(r_gpu[ok] - r64[ok]).max() < 2e-4, "residuals differ from the FP64 fit"
+    assert np.abs(r_gpu[well] - r64[well]).max() < 2e-4, "residuals differ from the FP64 fit"
