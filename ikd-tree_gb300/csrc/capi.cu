@@ -12,6 +12,7 @@
 #include <cstddef>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <new>
 #include <shared_mutex>
@@ -669,6 +670,21 @@ struct Tree {
         finish_update(nullptr, nullptr, 0);
     }
 
+    // True when every non-null pointer is page-locked host memory (registered
+    // with or allocated by CUDA).
+    static bool all_pinned(std::initializer_list<const void*> ptrs) {
+        for (const void* p : ptrs) {
+            if (p == nullptr) continue;
+            cudaPointerAttributes a{};
+            if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            if (a.type != cudaMemoryTypeHost) return false;
+        }
+        return true;
+    }
+
     // ---- concurrent small searches ------------------------------------------------
     // A search context: a stream, a device buffer (a status block for the
     // kernel's error bits, the result rows, the kNN scratch) and a pinned host
@@ -799,10 +815,14 @@ struct Tree {
             return;
         }
         reset_counters();
-        if (host_mode == 2) {
-            // Kernels read the queries and write the results in host memory.
+        if (host_mode == 2 || (host_mode == 1 && all_pinned({ids, d2, xyz, cnt}))) {
+            // Kernels read the queries and write the results in host memory:
+            // each warp's rows leave as coalesced 16-byte spans, so the
+            // transfer over the chip link overlaps the search instead of
+            // following it as one copy.
             small.ensure(knn_temp_bytes(nq, k) + 256, stream);
-            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, small.p, knn_lanes, bin_bits_for(nq), stream);
+            launch_knn(dt, q, stride, nq, k, lim, ids, d2, xyz, cnt, small.p, knn_lanes, bin_bits_for(nq), stream,
+                       /*host_out=*/true);
             read_status();
             if (st->err & ERR_STACK) throw Internal{"knn: traversal stack overflow"};
             return;
@@ -1150,8 +1170,12 @@ struct Batch {
     // Range requests in one pass: each query walked once with its hits staged
     // in a batch-wide array, then copied to their CSR places once the counts
     // are scanned (instead of a counting walk and a writing walk).  If the
-    // staging array overflows, the writing walk runs as before.
-    bool use_stage = true;
+    // staging array overflows, the writing walk runs as before.  Off by
+    // default: the counting walk runs beside the kNN classes on their graph
+    // branches, so removing it shortened nothing while the single pass and
+    // its copy lengthened the branch that ends the run (measured on 64 maps,
+    // 1.37M queries: 9.96 ms against 7.98 ms).
+    bool use_stage = false;
     long long stage_hits = 0;  // staging slots (0: the requests' capacities plus per-warp slack)
     std::vector<Req> reqs;  // in the order added
     std::mutex mu;

@@ -76,9 +76,11 @@ cudaError_t noalloc_scratch(int device, void** ptr);
 size_t noalloc_scratch_bytes();
 // `lanes` (1, 2 or 4) threads cooperate on each query; `bin_bits` (0 = off,
 // at most QBIN_BITS) levels of the tree order the queries before the search.
+// host_out: the outputs are host memory the GPU writes directly (each warp's
+// rows then leave as coalesced 16-byte spans through shared memory).
 void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq,
                 int* out_id, float* out_d2, float* out_xyz, int* out_cnt, void* temp, int lanes, int bin_bits,
-                cudaStream_t s);
+                cudaStream_t s, bool host_out = false);
 // Box (mode 0) and radius (mode 1) search.  Pass 1 (ids == nullptr) writes
 // per-query hit counts into `counts`; pass 2 writes ids / xyz starting at
 // offsets[i].  Boxes are {min xyz, max xyz}; radius queries are {x, y, z} with

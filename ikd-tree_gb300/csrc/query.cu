@@ -16,20 +16,18 @@ using search::FINF;
 #define IKDG_KNN_THREADS 128
 #endif
 constexpr int KNN_THREADS = IKDG_KNN_THREADS;
-// 1: kNN rows of k <= 8 leave a warp through shared memory as coalesced spans
-#ifndef IKDG_KNN_STAGED_OUT
-#define IKDG_KNN_STAGED_OUT 1
-#endif
-constexpr bool KNN_STAGED_OUT = IKDG_KNN_STAGED_OUT != 0;
 
-template <int KMAX, int G>
+
+// STAGED: the outputs are host memory (rows leave through shared memory as
+// coalesced 16-byte stores; see knn_body).
+template <int KMAX, int G, bool STAGED = false>
 __global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
                                                   long long nq, int k, float max_sq, int* __restrict__ out_id,
                                                   float* __restrict__ out_d2, float* __restrict__ out_xyz,
                                                   int* __restrict__ out_cnt, int* __restrict__ slots,
                                                   const int* __restrict__ perm) {
     const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if constexpr (KMAX > 0 && G == 1 && KNN_STAGED_OUT) {
+    if constexpr (KMAX > 0 && G == 1 && STAGED) {
         // rows of a warp's consecutive queries leave through shared memory
         __shared__ __align__(16) float stage[KNN_THREADS / 32][search::knn_stage_floats(KMAX)];
         search::knn_body<KMAX, G>(t, gtid, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm,
@@ -75,9 +73,17 @@ inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) /
 
 template <int KMAX>
 void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
-                float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s) {
+                float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s,
+                bool host_out = false) {
     const int G = lanes >= 4 ? 4 : lanes == 2 ? 2 : 1;
     const unsigned grid = blocks_for(nq * G, KNN_THREADS);
+    if constexpr (KMAX > 0) {
+        if (host_out && G == 1 && perm == nullptr) {
+            knn_kernel<KMAX, 1, true><<<grid, KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
+                                                                   out_xyz, out_cnt, slots, perm);
+            return;
+        }
+    }
 #define IKDG_KNN_G(GG)                                                                                              \
     knn_kernel<KMAX, GG><<<grid, KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, \
                                                       slots, perm)
@@ -174,7 +180,8 @@ size_t knn_temp_bytes(long long nq, int k) {
 }
 
 void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
-                float* out_d2, float* out_xyz, int* out_cnt, void* temp, int lanes, int bin_bits, cudaStream_t s) {
+                float* out_d2, float* out_xyz, int* out_cnt, void* temp, int lanes, int bin_bits, cudaStream_t s,
+                bool host_out) {
     if (nq <= 0) return;
     char* tp = (char*)temp;
     const int* perm = nullptr;
@@ -195,7 +202,7 @@ void launch_knn(const DevTree& t, const float* q, int q_stride, long long nq, in
     }
     int* slots = k > KNN_SMEM_MAX ? (int*)tp : nullptr;
 #define IKDG_KNN(KM) \
-    knn_launch<KM>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm, lanes, s)
+    knn_launch<KM>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm, lanes, s, host_out)
     if (k > KNN_SMEM_MAX)
         IKDG_KNN(0);
     else if (k > KNN_REG_MAX)

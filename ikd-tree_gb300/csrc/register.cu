@@ -7,6 +7,9 @@
 //
 //   w_i = R(omega) p_i + t                      (scan point to map frame)
 //   plane through the k neighbours of w_i:      min |A x + 1|^2,  A = [m_j^T]
+//     (solved by an orthogonal factorisation, as FAST-LIO2's QR solve: the
+//     normal equations square the condition number of A, which is large for
+//     planes far from the origin or nearly through it)
 //   n_i = x / |x|,  d_i = 1 / |x|               (plane n . q + d = 0)
 //   valid_i  if every |n_i . m_j + d_i| <= plane_thresh
 //   r_i = n_i . w_i + d_i,   L = 1/2 sum_valid r_i^2
@@ -41,7 +44,40 @@ __global__ void transform_kernel(const float* __restrict__ p, long long n, const
     for (int r = 0; r < 3; ++r) w[3 * i + r] = (float)wd[r];
 }
 
-// Plane fit (3x3 normal equations solved by Cramer's rule) and residual.
+// Least squares min |A x - b| for the k rows of A (k x 3) and b by a QR
+// factorisation built one row at a time with Givens rotations (R upper
+// triangular 3 x 3, z = Q^T b), then back substitution.  Returns false when R
+// is singular.
+__device__ __forceinline__ bool lsq3_givens(const float* __restrict__ rows, int k, double b_all, double x[3]) {
+    double R[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double z[3] = {0, 0, 0};
+    for (int j = 0; j < k; ++j) {
+        double r[3] = {rows[3 * j], rows[3 * j + 1], rows[3 * j + 2]};
+        double b = b_all;
+        for (int c = 0; c < 3; ++c) {
+            if (r[c] == 0.0) continue;
+            const double h = hypot(R[c][c], r[c]);
+            const double cs = R[c][c] / h, sn = r[c] / h;
+            for (int m = c; m < 3; ++m) {
+                const double t = cs * R[c][m] + sn * r[m];
+                r[m] = -sn * R[c][m] + cs * r[m];
+                R[c][m] = t;
+            }
+            const double t = cs * z[c] + sn * b;
+            b = -sn * z[c] + cs * b;
+            z[c] = t;
+        }
+    }
+    const double scale = fmax(fabs(R[0][0]), fmax(fabs(R[1][1]), fabs(R[2][2])));
+    for (int c = 0; c < 3; ++c)
+        if (!(fabs(R[c][c]) > 1e-12 * scale)) return false;
+    x[2] = z[2] / R[2][2];
+    x[1] = (z[1] - R[1][2] * x[2]) / R[1][1];
+    x[0] = (z[0] - R[0][1] * x[1] - R[0][2] * x[2]) / R[0][0];
+    return true;
+}
+
+// Plane fit (least squares by Givens QR) and residual.
 __global__ void plane_residual_kernel(const float* __restrict__ p, const double* __restrict__ Rt, long long n, int k,
                                       const float* __restrict__ nb, const int* __restrict__ cnt, float thresh,
                                       float4* __restrict__ planes, float* __restrict__ res, int* __restrict__ valid) {
@@ -51,21 +87,10 @@ __global__ void plane_residual_kernel(const float* __restrict__ p, const double*
     float4 pc = make_float4(0.f, 0.f, 0.f, 0.f);
     int ok = 0;
     float r = 0.f;
-    if (cnt[i] >= k && k >= 3) {
-        double a00 = 0, a01 = 0, a02 = 0, a11 = 0, a12 = 0, a22 = 0, b0 = 0, b1 = 0, b2 = 0;
-        for (int j = 0; j < k; ++j) {
-            const double x = nb[(i * k + j) * 3], y = nb[(i * k + j) * 3 + 1], z = nb[(i * k + j) * 3 + 2];
-            a00 += x * x; a01 += x * y; a02 += x * z;
-            a11 += y * y; a12 += y * z; a22 += z * z;
-            b0 -= x; b1 -= y; b2 -= z;
-        }
-        const double c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
-        const double det = a00 * c00 + a01 * c01 + a02 * c02;
-        if (fabs(det) > 1e-30) {
-            const double c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
-            const double x0 = (c00 * b0 + c01 * b1 + c02 * b2) / det;
-            const double x1 = (c01 * b0 + c11 * b1 + c12 * b2) / det;
-            const double x2 = (c02 * b0 + c12 * b1 + c22 * b2) / det;
+    double xs[3];
+    if (cnt[i] >= k && k >= 3 && lsq3_givens(nb + i * k * 3, k, -1.0, xs)) {
+        {
+            const double x0 = xs[0], x1 = xs[1], x2 = xs[2];
             const double nrm = sqrt(x0 * x0 + x1 * x1 + x2 * x2);
             if (nrm > 0) {
                 const double nx = x0 / nrm, ny = x1 / nrm, nz = x2 / nrm, dd = 1.0 / nrm;

@@ -36,15 +36,6 @@ __device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4&
 #endif
 constexpr int RANGE_LEAF_BATCH = IKDG_RANGE_LEAF_BATCH;
 
-// kNN: lanes of a warp holding a leaf that end the node phase early (32: the
-// node phase runs until every lane holds a leaf or is done).
-#ifndef IKDG_KNN_LEAF_T
-#define IKDG_KNN_LEAF_T 32
-#endif
-constexpr int KNN_LEAF_T = IKDG_KNN_LEAF_T;
-#ifndef IKDG_KNN_KEY64
-#define IKDG_KNN_KEY64 0
-#endif
 
 // Stores n floats (or int bits) from shared memory to dst with the whole warp:
 // 16-byte stores where dst is 16-byte aligned, lane-consecutive 4-byte stores
@@ -102,15 +93,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     const float qz = valid ? q[qi * q_stride + 2] : 0.f;
 
     constexpr int KR = KMAX > 0 ? KMAX : 1;
-#if IKDG_KNN_KEY64
-    unsigned long long bkey[KR];
-    int bsl[KR];
-#pragma unroll
-    for (int j = 0; j < KR; ++j) {
-        bkey[j] = 0x7f8000007fffffffull;  // (+inf, largest id)
-        bsl[j] = -1;
-    }
-#else
     float bd[KR];
     int bi[KR], bsl[KR];
 #pragma unroll
@@ -119,7 +101,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         bi[j] = 0x7fffffff;
         bsl[j] = -1;
     }
-#endif
     const bool in_rows = kd == nullptr;
     float* gd = in_rows ? out_d2 + qi * k : kd;
     int* gi = in_rows ? out_id + qi * k : ki;
@@ -176,28 +157,6 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
             }
             return;
         }
-#if IKDG_KNN_KEY64
-        // (distance, id) as one 64-bit key: distances are >= 0, so their bit
-        // patterns order like the floats and the id breaks ties.
-        unsigned long long ck = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
-        int cs = sl;
-#pragma unroll
-        for (int m = 0; m < KR; ++m) {
-            const bool sw = ck < bkey[m];
-            const unsigned long long tk = bkey[m];
-            const int ts = bsl[m];
-            bkey[m] = sw ? ck : tk;
-            bsl[m] = sw ? cs : ts;
-            ck = sw ? tk : ck;
-            cs = sw ? ts : cs;
-        }
-#pragma unroll
-        for (int m = 0; m < KR; ++m)
-            if (m == k - 1) {
-                worst = __uint_as_float((unsigned)(bkey[m] >> 32));
-                worst_id = (int)(unsigned)bkey[m];
-            }
-#else
         float cd = d;
         int cid = id, cs = sl;
 #pragma unroll
@@ -218,17 +177,13 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 worst = bd[m];
                 worst_id = bi[m];
             }
-#endif
     };
 
     while (true) {
-        // Node phase: ends when no lane has node work left, or when at least
-        // KNN_LEAF_T lanes hold a leaf (then those leaves are scanned while the
-        // other lanes wait, instead of the holders waiting for the longest walk).
+        // Node phase.
         while (true) {
             const bool nodework = !done && cur >= 0;
             if (!__any_sync(0xffffffffu, nodework)) break;
-            if (KNN_LEAF_T < 32 && __popc(__ballot_sync(0xffffffffu, !done && cur < 0)) >= KNN_LEAF_T) break;
             if (!nodework) continue;
             if (++visits > MAX_VISITS) {
                 atomicOr(&t.st->err, ERR_LOOP);
@@ -335,13 +290,8 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 for (int j = 0; j < KR; ++j) {
                     if (j < k) {
                         const bool ok = bsl[j] >= 0;
-#if IKDG_KNN_KEY64
-                        const int id = ok ? (int)(unsigned)bkey[j] : -1;
-                        const float dd = ok ? __uint_as_float((unsigned)(bkey[j] >> 32)) : FINF;
-#else
                         const int id = ok ? bi[j] : -1;
                         const float dd = ok ? bd[j] : FINF;
-#endif
                         s_id[lane * k + j] = __int_as_float(id);
                         s_d2[lane * k + j] = dd;
                         if (out_xyz != nullptr) {
@@ -386,13 +336,8 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     for (int j = 0; j < KR; ++j) {
         if (j < k) {
             const bool ok = bsl[j] >= 0;
-#if IKDG_KNN_KEY64
-            out_id[qi * k + j] = ok ? (int)(unsigned)bkey[j] : -1;
-            out_d2[qi * k + j] = ok ? __uint_as_float((unsigned)(bkey[j] >> 32)) : FINF;
-#else
             out_id[qi * k + j] = ok ? bi[j] : -1;
             out_d2[qi * k + j] = ok ? bd[j] : FINF;
-#endif
             if (out_xyz != nullptr) {
                 float4 p = ok ? __ldg(P + bsl[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
                 out_xyz[(qi * k + j) * 3 + 0] = p.x;

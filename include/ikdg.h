@@ -198,12 +198,12 @@ int ikdg_batch_set_graph(ikdg_batch* b, int use_graph);
  * nearby nodes; results are unchanged and stay in query order.  0: queries
  * are searched in the order given. */
 int ikdg_batch_set_query_order(ikdg_batch* b, int ordered);
-/* single_pass 1 (default): box / radius requests walk each query once, stage
- * its hits in a batch-wide array (hit_capacity slots; 0 = the requests'
- * capacities plus per-warp slack) and copy them to their CSR places after the
- * count scan; if the staging array overflows, the run falls back to writing
- * every range request by a second walk, with the same results.  0: a counting
- * walk and a writing walk, as the per-call path does. */
+/* single_pass 1: box / radius requests walk each query once, stage its hits
+ * in a batch-wide array (hit_capacity slots; 0 = the requests' capacities
+ * plus per-warp slack) and copy them to their CSR places after the count
+ * scan; if the staging array overflows, the run falls back to writing every
+ * range request by a second walk, with the same results.  0 (default): a
+ * counting walk and a writing walk, as the per-call path does. */
 int ikdg_batch_set_range_staging(ikdg_batch* b, int single_pass, int64_t hit_capacity);
 /* Asynchronous on the batch's stream. */
 int ikdg_batch_run(ikdg_batch* b);

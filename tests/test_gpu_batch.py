@@ -228,15 +228,15 @@ def test_batch_query_order_changes_nothing(scene):
 
 
 def test_batch_range_passes_agree(scene):
-    """Range requests in one walk with staged hits (the default), with a
-    staging array too small (the run falls back to the writing walk), and as
-    a counting walk plus a writing walk: the same bytes as the per-call path."""
+    """Range requests in one walk with staged hits, with a staging array too
+    small (the run falls back to the writing walk), and as a counting walk
+    plus a writing walk (the default): the same bytes as the per-call path."""
     maps, trees, empty, reqs, b = scene
     ref = per_call(reqs)
     for single, cap in ((True, 0), (True, 1000), (False, 0)):
         b.set_range_staging(single, cap)
         assert_same(batched(b, reqs), ref, reqs)
-    b.set_range_staging(True, 0)
+    b.set_range_staging(False, 0)
 
 
 def test_batch_range_requests_match_oracle(scene):
