@@ -427,9 +427,9 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
     b.set_query_order(False)
     batch_unordered_ms = timed(batched)
     b.set_query_order(True)
-    b.set_range_staging(True)
-    batch_single_pass_ms = timed(batched)
-    b.set_range_staging(False)
+    b.set_range_mode(False)
+    batch_two_pass_ms = timed(batched)
+    b.set_range_mode(True)
     batch_ms = timed(batched)
     batch_dev = batch_device_ms()
     tuned = None
@@ -459,9 +459,9 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
         "batched_unordered_ms": batch_unordered_ms,
         "batched_unordered": "the same batch with every request's queries searched in the given order "
                              "(query ordering off)",
-        "batched_single_pass_ms": batch_single_pass_ms,
-        "batched_single_pass": "the same batch with every range query walked once, hits staged and copied "
-                               "after the count scan",
+        "batched_two_pass_ms": batch_two_pass_ms,
+        "batched_two_pass": "the same batch with box / radius requests as a counting walk, a prefix sum and a "
+                            "writing walk (the per-call scheme) instead of the fused kernel",
         "speedup_vs_plain": plain_ms / batch_ms,
         "speedup_vs_plain_sync": plain_sync_ms / batch_ms,
         "autotuned": tuned,

@@ -91,19 +91,95 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
     }
 }
 
-// Phase 1 of the range requests, single pass: every query walked once in
-// write mode, its hits staged (search.cuh RangeStage) and its hit count stored
-// in counts[cbase + qi].
-__global__ void __launch_bounds__(BATCH_THREADS) batch_range_stage_kernel(const DevTree* __restrict__ trees,
+// Look-back states of a chunk's word: total not known yet, the chunk's own
+// total (aggregate), or the total of the request's chunks up to and including
+// it (inclusive).  The value sits above the two state bits.
+constexpr unsigned long long CS_EMPTY = 0, CS_AGG = 1, CS_INCL = 2;
+constexpr int LOOKBACK_SPINS = 1 << 20;
+
+__device__ __forceinline__ unsigned long long load_chunk_state(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.global.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void store_chunk_state(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.global.release.gpu.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Range requests, fused: count, look back for the chunk's offset, write.
+template <int MODE>
+__device__ __forceinline__ void fused_range_chunk(const DevTree& t, const BatchReq& R, long long c, long long ci,
+                                                  long long c_begin, unsigned long long* __restrict__ cstat) {
+    const int lane = threadIdx.x & 31;
+    const long long qi = (c - R.c1) * BATCH_CHUNK + lane;
+    const bool valid = qi < R.nq;
+    const long long n = search::range_body<MODE, search::RANGE_COUNT>(t, R.q, R.q_stride, R.radius, R.r_stride, qi,
+                                                                     valid, 0, 0, nullptr, nullptr);
+    long long incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const long long total = __shfl_sync(0xffffffffu, incl, 31);
+    long long prefix = 0;
+    if (lane == 0) {
+        if (c == R.c1) {
+            store_chunk_state(cstat + ci, ((unsigned long long)total << 2) | CS_INCL);
+        } else {
+            store_chunk_state(cstat + ci, ((unsigned long long)total << 2) | CS_AGG);
+            // every earlier chunk of the request was taken by a running warp
+            // and publishes its total right after its counting walk
+            long long p = ci - 1;
+            int spins = 0;
+            while (true) {
+                const unsigned long long w = load_chunk_state(cstat + p);
+                const unsigned long long st = w & 3ull;
+                if (st == CS_EMPTY) {
+                    if (++spins > LOOKBACK_SPINS) {
+                        atomicOr(&t.st->err, ERR_LOOP);
+                        prefix = -1;
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                prefix += (long long)(w >> 2);
+                if (st == CS_INCL || p + c_begin <= R.c1) break;
+                --p;
+            }
+            if (prefix >= 0) store_chunk_state(cstat + ci, ((unsigned long long)(prefix + total) << 2) | CS_INCL);
+        }
+    }
+    prefix = __shfl_sync(0xffffffffu, prefix, 0);
+    if (prefix < 0) return;  // gave up waiting (error raised): nothing written
+    const long long o = prefix + incl - n;
+    bool go = valid;
+    if (valid) {
+        R.offsets[qi] = o;
+        if (qi == R.nq - 1) {
+            R.offsets[R.nq] = o + n;
+            if (R.total != nullptr) *R.total = o + n;
+        }
+        if (n == 0 || R.ids == nullptr) {
+            go = false;
+        } else if (o + n > R.capacity) {
+            atomicOr(&t.st->err, ERR_OUTPUT);
+            go = false;
+        }
+    }
+    search::range_body<MODE, search::RANGE_WRITE>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, go, o, o + n, R.ids,
+                                                  R.xyz);
+}
+
+__global__ void __launch_bounds__(BATCH_THREADS) batch_range_fused_kernel(const DevTree* __restrict__ trees,
                                                                           const BatchReq* __restrict__ reqs,
                                                                           const long long* __restrict__ req_c1,
                                                                           int r0, int r1, long long c_begin,
                                                                           long long c_end,
-                                                                          long long* __restrict__ counts,
                                                                           unsigned long long* __restrict__ ctr,
-                                                                          search::RangeStage st) {
+                                                                          unsigned long long* __restrict__ cstat) {
     const int lane = threadIdx.x & 31;
-    search::StageCursor cur;
     for (;;) {
         long long c = 0;
         int r = -1;
@@ -116,90 +192,22 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_range_stage_kernel(const 
         if (c >= c_end) break;
         const BatchReq& R = reqs[r];
         const DevTree t = trees[R.tree];
-        long long qi = (c - R.c1) * BATCH_CHUNK + lane;
-        const bool valid = qi < R.nq;
-        if (valid && R.perm != nullptr) qi = __ldg(R.perm + qi);
-        search::RangeStage rs = st;
-        rs.qbase = (int)R.cbase;
-        const long long n =
-            R.kind == BATCH_BOX
-                ? search::range_body<0, search::RANGE_STAGE>(t, R.q, R.q_stride, nullptr, 0, qi, valid, 0, 0, nullptr,
-                                                             nullptr, &rs, &cur)
-                : search::range_body<1, search::RANGE_STAGE>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, valid, 0,
-                                                             0, nullptr, nullptr, &rs, &cur);
-        if (valid) counts[R.cbase + qi] = n;
-    }
-    if (lane == 0) search::stage_close(st, cur);
-}
-
-// After the count scan: each range query's CSR offset (and each request's
-// total); a query whose results would end past its request's capacity raises
-// ERR_OUTPUT (its hits are not copied).  rq_base: batch-global first query of
-// every range request, ascending; rq_req: the request.
-__global__ void batch_offsets_kernel(const DevTree* __restrict__ trees, const BatchReq* __restrict__ reqs,
-                                     const long long* __restrict__ rq_base, const int* __restrict__ rq_req, int nr,
-                                     long long n_range, const long long* __restrict__ goff) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n_range) return;
-    const int j = find_req(rq_base, 0, nr, g);
-    const BatchReq& R = reqs[rq_req[j]];
-    const long long qi = g - R.cbase;
-    const long long base = goff[R.cbase];
-    const long long o = goff[g] - base, e = goff[g + 1] - base;
-    R.offsets[qi] = o;
-    if (qi == R.nq - 1) {
-        R.offsets[R.nq] = e;
-        if (R.total != nullptr) *R.total = e;
-    }
-    if (e > o && R.ids != nullptr && e > R.capacity) atomicOr(&trees[R.tree].st->err, ERR_OUTPUT);
-}
-
-// Moves the staged hits to their CSR places: one warp per run record.
-__global__ void __launch_bounds__(BATCH_THREADS) batch_copy_kernel(const BatchReq* __restrict__ reqs,
-                                                                   const long long* __restrict__ rq_base,
-                                                                   const int* __restrict__ rq_req, int nr,
-                                                                   const long long* __restrict__ goff,
-                                                                   search::RangeStage st) {
-    if (*st.overflow) return;  // the direct write pass rewrites every range request
-    const int lane = threadIdx.x & 31;
-    const long long nruns = min((long long)*st.run_ctr, st.run_cap);
-    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = w0; w < nruns; w += nw) {
-        const int4 run = st.runs[w];
-        if (run.z <= 0) continue;
-        const long long g = run.x;
-        const int j = find_req(rq_base, 0, nr, g);
-        const BatchReq& R = reqs[rq_req[j]];
-        if (R.ids == nullptr) continue;
-        const long long base = goff[R.cbase];
-        if (goff[g + 1] - base > R.capacity) continue;
-        if (lane < run.z) {
-            const float4 h = st.hits[(long long)run.y + lane];
-            const long long d = goff[g] - base + run.w + lane;
-            R.ids[d] = (int)__float_as_uint(h.w);
-            if (R.xyz != nullptr) {
-                R.xyz[3 * d] = h.x;
-                R.xyz[3 * d + 1] = h.y;
-                R.xyz[3 * d + 2] = h.z;
-            }
-        }
+        if (R.kind == BATCH_BOX)
+            fused_range_chunk<0>(t, R, c, c - c_begin, c_begin, cstat);
+        else
+            fused_range_chunk<1>(t, R, c, c - c_begin, c_begin, cstat);
     }
 }
 
-// Phase 2 (two-pass form, and the single pass's fallback when its staging
-// overflowed; with only_if set it runs only when *only_if != 0): range
-// requests write their CSR offsets and, where the request's capacity holds
-// the query's results, the ids / points.
+// Phase 2: range requests write their CSR offsets and, where the request's
+// capacity holds the query's results, the ids / points.
 __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTree* __restrict__ trees,
                                                                     const BatchReq* __restrict__ reqs,
                                                                     const int* __restrict__ ridx,
                                                                     const long long* __restrict__ req_c2, int nr,
                                                                     long long c_end,
                                                                     const long long* __restrict__ goff,
-                                                                    unsigned long long* __restrict__ ctr,
-                                                                    const int* __restrict__ only_if) {
-    if (only_if != nullptr && *only_if == 0) return;
+                                                                    unsigned long long* __restrict__ ctr) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         long long c = 0;
@@ -360,34 +368,6 @@ int batch_write_grid() {
     return resident_grid((const void*)batch_write_kernel);
 }
 
-int batch_stage_grid() {
-    std::lock_guard<std::mutex> lock(g_grid_mu);
-    return resident_grid((const void*)batch_range_stage_kernel);
-}
-
-void launch_batch_range_stage(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
-                              long long c_begin, long long c_end, long long* counts, unsigned long long* ctr,
-                              const search::RangeStage& st, int grid, cudaStream_t s) {
-    if (c_end <= c_begin || r1 <= r0) return;
-    const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
-    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
-    batch_range_stage_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr,
-                                                         st);
-}
-
-void launch_batch_offsets(const DevTree* trees, const BatchReq* reqs, const long long* rq_base, const int* rq_req,
-                          int nr, long long n_range, const long long* goff, cudaStream_t s) {
-    if (n_range <= 0 || nr <= 0) return;
-    batch_offsets_kernel<<<(unsigned)((n_range + 255) / 256), 256, 0, s>>>(trees, reqs, rq_base, rq_req, nr, n_range,
-                                                                           goff);
-}
-
-void launch_batch_copy(const BatchReq* reqs, const long long* rq_base, const int* rq_req, int nr,
-                       const long long* goff, const search::RangeStage& st, int grid, cudaStream_t s) {
-    if (nr <= 0) return;
-    batch_copy_kernel<<<grid, BATCH_THREADS, 0, s>>>(reqs, rq_base, rq_req, nr, goff, st);
-}
-
 void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
                          long long c_begin, long long c_end, int kclass, int lanes, long long* counts,
                          unsigned long long* ctr, int grid, cudaStream_t s) {
@@ -395,6 +375,20 @@ void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long 
     const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
     const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
     search_dispatch(kclass, lanes, true, nullptr, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
+}
+
+int batch_fused_grid() {
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    return resident_grid((const void*)batch_range_fused_kernel);
+}
+
+void launch_batch_range_fused(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
+                              long long c_begin, long long c_end, unsigned long long* ctr,
+                              unsigned long long* cstat, int grid, cudaStream_t s) {
+    if (c_end <= c_begin || r1 <= r0) return;
+    const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
+    batch_range_fused_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, ctr, cstat);
 }
 
 void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long long* qstart, int n, long long total,
@@ -405,12 +399,11 @@ void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long lo
 }
 
 void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
-                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s,
-                        const int* only_if) {
+                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s) {
     if (c_end <= 0 || nr <= 0) return;
     const long long ctas = (c_end + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
     const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
-    batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr, only_if);
+    batch_write_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, ridx, req_c2, nr, c_end, goff, ctr);
 }
 
 }  // namespace ikdg

@@ -1167,16 +1167,12 @@ struct Batch {
     // so the lanes of a warp walk nearby nodes and leaves.  Results stay in
     // query order.
     bool use_order = true;
-    // Range requests in one pass: each query walked once with its hits staged
-    // in a batch-wide array, then copied to their CSR places once the counts
-    // are scanned (instead of a counting walk and a writing walk).  If the
-    // staging array overflows, the writing walk runs as before.  Off by
-    // default: the counting walk runs beside the kNN classes on their graph
-    // branches, so removing it shortened nothing while the single pass and
-    // its copy lengthened the branch that ends the run (measured on 64 maps,
-    // 1.37M queries: 9.96 ms against 7.98 ms).
-    bool use_stage = false;
-    long long stage_hits = 0;  // staging slots (0: the requests' capacities plus per-warp slack)
+    // Range requests: 1 (default) one kernel in which each warp counts its
+    // chunk, takes its CSR offset by a look-back over the request's earlier
+    // chunks and writes at once, while the nodes and leaves it walked are
+    // still cached; 0: a counting walk over all range queries, one prefix sum,
+    // a writing walk (the per-call scheme).
+    int range_mode = 1;
     std::vector<Req> reqs;  // in the order added
     std::mutex mu;
     std::string err;
@@ -1208,12 +1204,11 @@ struct Batch {
     uint32_t* d_okeys[2] = {nullptr, nullptr};
     uint32_t* d_ovals[2] = {nullptr, nullptr};
     void* d_osort = nullptr;
-    // single-pass range requests (use_stage)
-    bool staged = false;
-    search::RangeStage stage{};
-    long long* d_rq_base = nullptr;
-    int* d_rq_req = nullptr;
-    int n_rq = 0, stage_grid = 0;
+    // fused range requests (range_mode 1): per-chunk look-back words
+    bool fused = false;
+    unsigned long long* d_cstat = nullptr;
+    long long n_rchunks = 0, range_c_begin = 0;
+    int fused_grid = 0;
     DevStatus* d_st = nullptr;
     DevTree* h_trees = nullptr;      // pinned: read by the graph's first copy
     DevStatus* h_st = nullptr;       // pinned
@@ -1356,30 +1351,15 @@ struct Batch {
         c2_end = chunk2;
         for (auto& g : groups) g.grid = batch_search_grid(g.kclass, g.lanes);
         write_grid = batch_write_grid();
-        // range requests in ascending cbase (sorted order), for the offsets
-        // and copy kernels of the single pass
-        std::vector<long long> rq_base;
-        std::vector<int> rq_req;
-        long long cap_sum = 0;
-        for (int p = 0; p < n; ++p)
-            if (d[p].kind != BATCH_KNN) {
-                rq_base.push_back(d[p].cbase);
-                rq_req.push_back(p);
-                if (d[p].ids != nullptr) cap_sum += std::min<long long>(d[p].capacity, (long long)1 << 40);
+        fused = range_mode == 1 && n_range_queries > 0;
+        n_rchunks = 0;
+        range_c_begin = 0;
+        for (auto& G : groups)
+            if (G.kclass == BATCH_RANGE_CLASS) {
+                if (n_rchunks == 0) range_c_begin = G.c_begin;
+                n_rchunks = G.c_end - range_c_begin;
             }
-        n_rq = (int)rq_base.size();
-        staged = use_stage && n_range_queries > 0;
-        long long hit_cap = 0, run_cap = 0;
-        if (staged) {
-            stage_grid = batch_stage_grid();
-            const long long warps = (long long)stage_grid * (BATCH_THREADS / 32);
-            hit_cap = std::min<long long>(cap_sum, (long long)1 << 28) + warps * search::STAGE_HIT_SEG;
-            run_cap = hit_cap / 2 + warps * search::STAGE_RUN_SEG;
-            if (stage_hits > 0) {
-                hit_cap = std::min<long long>(stage_hits, (long long)1 << 30);
-                run_cap = hit_cap / 2 + 1;
-            }
-        }
+        if (fused) fused_grid = batch_fused_grid();
         // one allocation for the plan
         const size_t nt = trees.size(), nr = range_reqs.size();
         size_t bytes = align_up(sizeof(DevTree) * nt) + align_up(sizeof(BatchReq) * n) +
@@ -1390,9 +1370,7 @@ struct Batch {
         const long long nqo = ordered ? n_queries : 0;
         bytes += align_up(sizeof(long long) * (n + 1)) + 4 * align_up(sizeof(uint32_t) * std::max<long long>(nqo, 1)) +
                  align_up(ordered ? sort_temp_bytes(nqo, 1) : 0);
-        bytes += align_up(sizeof(long long) * (n_rq + 1)) + align_up(sizeof(int) * (n_rq + 1)) +
-                 align_up(sizeof(float4) * std::max<long long>(hit_cap, 1)) +
-                 align_up(sizeof(int4) * std::max<long long>(run_cap, 1)) + align_up(sizeof(unsigned long long) * 4);
+        bytes += align_up(sizeof(unsigned long long) * std::max<long long>(n_rchunks, 1));
         CK(cudaMalloc(&dev, bytes));
         Carver c(dev);
         d_trees = c.take<DevTree>(nt);
@@ -1413,26 +1391,15 @@ struct Batch {
         }
         d_osort = ordered ? (void*)c.take<char>(sort_temp_bytes(nqo, 1)) : nullptr;
         for (int p = 0; p < n; ++p) d[p].perm = ordered ? (const int*)(d_ovals[0] + qstart[p]) : nullptr;
-        d_rq_base = c.take<long long>(n_rq + 1);
-        d_rq_req = c.take<int>(n_rq + 1);
-        stage.hits = c.take<float4>(std::max<long long>(hit_cap, 1));
-        stage.runs = c.take<int4>(std::max<long long>(run_cap, 1));
-        unsigned long long* sctr = c.take<unsigned long long>(4);
-        stage.hit_ctr = sctr;
-        stage.run_ctr = sctr + 1;
-        stage.overflow = (int*)(sctr + 2);
-        stage.hit_cap = hit_cap;
-        stage.run_cap = run_cap;
-        stage.qbase = 0;
+        d_cstat = c.take<unsigned long long>(std::max<long long>(n_rchunks, 1));
+        if (fused)  // the look-back gives CSR offsets in query order: no permutation
+            for (int p = 0; p < n; ++p)
+                if (d[p].kind != BATCH_KNN) d[p].perm = nullptr;
         for (size_t j = 0; j < nr; ++j) d[pos_of[range_reqs[j]]].total = d_totals + j;
         CK(cudaMallocHost(&h_trees, sizeof(DevTree) * std::max<size_t>(nt, 1)));
         CK(cudaMemcpyAsync(d_reqs, d.data(), sizeof(BatchReq) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(d_c1, c1.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(d_qstart, qstart.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
-        if (n_rq > 0) {
-            CK(cudaMemcpyAsync(d_rq_base, rq_base.data(), sizeof(long long) * n_rq, cudaMemcpyHostToDevice, stream));
-            CK(cudaMemcpyAsync(d_rq_req, rq_req.data(), sizeof(int) * n_rq, cudaMemcpyHostToDevice, stream));
-        }
         if (!ridx.empty()) {
             CK(cudaMemcpyAsync(d_c2, c2.data(), sizeof(long long) * c2.size(), cudaMemcpyHostToDevice, stream));
             CK(cudaMemcpyAsync(d_ridx, ridx.data(), sizeof(int) * ridx.size(), cudaMemcpyHostToDevice, stream));
@@ -1480,7 +1447,7 @@ struct Batch {
         CK(cudaMemcpyAsync(d_trees, h_trees, sizeof(DevTree) * trees.size(), cudaMemcpyHostToDevice, stream));
         CK(cudaMemsetAsync(d_ctr, 0, sizeof(unsigned long long) * 64, stream));
         CK(cudaMemsetAsync(d_st, 0, sizeof(DevStatus), stream));
-        if (staged) CK(cudaMemsetAsync(stage.hit_ctr, 0, sizeof(unsigned long long) * 3, stream));
+        if (fused) CK(cudaMemsetAsync(d_cstat, 0, sizeof(unsigned long long) * n_rchunks, stream));
         if (ordered) {
             launch_batch_keys(d_trees, d_reqs, d_qstart, (int)reqs.size(), n_queries, req_bits, d_okeys[0],
                               d_ovals[0], stream);
@@ -1492,26 +1459,18 @@ struct Batch {
             const Group& G = groups[g];
             cudaStream_t s = g == 0 ? stream : branch[g - 1];
             if (g > 0) CK(cudaStreamWaitEvent(s, ev_fork, 0));
-            if (staged && G.kclass == BATCH_RANGE_CLASS)
-                launch_batch_range_stage(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, d_counts, d_ctr + g,
-                                         stage, stage_grid, s);
+            if (fused && G.kclass == BATCH_RANGE_CLASS)
+                launch_batch_range_fused(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, d_ctr + g,
+                                         d_cstat + (G.c_begin - range_c_begin), fused_grid, s);
             else
                 launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes,
                                     d_counts, d_ctr + g, G.grid, s);
             if (g > 0) CK(cudaEventRecord(ev_join[g - 1], s));
         }
         for (size_t g = 1; g < groups.size(); ++g) CK(cudaStreamWaitEvent(stream, ev_join[g - 1], 0));
-        if (nridx > 0) {
+        if (nridx > 0 && !fused) {
             exclusive_scan(d_counts, d_goff, n_range_queries + 1, nullptr, d_scan, stream);
-            if (staged) {
-                launch_batch_offsets(d_trees, d_reqs, d_rq_base, d_rq_req, n_rq, n_range_queries, d_goff, stream);
-                launch_batch_copy(d_reqs, d_rq_base, d_rq_req, n_rq, d_goff, stage, write_grid, stream);
-                launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid,
-                                   stream, stage.overflow);
-            } else {
-                launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid,
-                                   stream);
-            }
+            launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid, stream);
         }
         // range requests without queries: empty CSR
         for (int j : range_reqs)
@@ -2166,12 +2125,10 @@ int ikdg_batch_set_query_order(ikdg_batch* h, int ordered) {
     });
 }
 
-int ikdg_batch_set_range_staging(ikdg_batch* h, int single_pass, int64_t hit_capacity) {
+int ikdg_batch_set_range_mode(ikdg_batch* h, int fused) {
     return batch_guarded(h, [&](ikdg::Batch& b) {
-        if (hit_capacity < 0) throw ikdg::BadArg{"batch: negative staging capacity"};
         b.drop_plan();
-        b.use_stage = single_pass != 0;
-        b.stage_hits = hit_capacity;
+        b.range_mode = fused != 0 ? 1 : 0;
     });
 }
 

@@ -143,27 +143,19 @@ void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long lo
                        int req_bits, uint32_t* keys, uint32_t* vals, cudaStream_t s);
 // Phase 2 over the range requests listed in ridx[0..nr) (ascending c2, chunks
 // [0, c_end)); goff: exclusive scan of the batch count array.
-// only_if (nullable): the kernel does nothing unless *only_if != 0 (the
-// fallback of the single pass below).
 void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
-                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s,
-                        const int* only_if = nullptr);
-// Single-pass range requests (search.cuh RangeStage): phase 1 walks every
-// query once, staging its hits and storing its count; after the count scan the
-// offsets kernel writes every query's CSR offset and the copy kernel moves the
-// staged hits.  rq_base / rq_req: first batch-global query and request of
-// every range request (ascending).
-namespace search {
-struct RangeStage;
-}
-int batch_stage_grid();
-void launch_batch_range_stage(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
-                              long long c_begin, long long c_end, long long* counts, unsigned long long* ctr,
-                              const search::RangeStage& st, int grid, cudaStream_t s);
-void launch_batch_offsets(const DevTree* trees, const BatchReq* reqs, const long long* rq_base, const int* rq_req,
-                          int nr, long long n_range, const long long* goff, cudaStream_t s);
-void launch_batch_copy(const BatchReq* reqs, const long long* rq_base, const int* rq_req, int nr,
-                       const long long* goff, const search::RangeStage& st, int grid, cudaStream_t s);
+                        long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s);
+// Range requests in one kernel: each warp counts its chunk's hits, takes the
+// chunk's CSR offset from the chunks of the same request before it (a
+// look-back over per-chunk totals: chunks are taken in order, so every chunk
+// it waits for belongs to a running warp) and writes its hits right away,
+// while the walked nodes and leaves are still in cache.  cstat: one zeroed
+// word per chunk of [c_begin, c_end).  Requests must run in query order (no
+// permutation).  A look-back that waits too long raises ERR_LOOP.
+int batch_fused_grid();
+void launch_batch_range_fused(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
+                              long long c_begin, long long c_end, unsigned long long* ctr,
+                              unsigned long long* cstat, int grid, cudaStream_t s);
 
 // ---- register.cu ---------------------------------------------------------------
 // Rt_dev: 12 doubles, R row-major then t.  planes: 2 float4 per point ({n,d}

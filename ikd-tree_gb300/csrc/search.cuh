@@ -350,39 +350,10 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
     if (out_cnt != nullptr) out_cnt[qi] = cnt;
 }
 
-// Staging output of the single-pass range search of multi-tree batches
-// (OUT == RANGE_STAGE): every leaf step's hits go to a batch-wide staging
-// array in segments a warp claims with one atomic, and one run record
-// {query, staging position, hits, position within the query} per step lets a
-// copy kernel move them to their CSR place once the counts are known.
-struct RangeStage {
-    float4* hits;                    // {x, y, z, id}
-    long long hit_cap;
-    unsigned long long* hit_ctr;     // staging slots claimed
-    int4* runs;                      // {query (batch-global), staging position, hits, position in query}
-    long long run_cap;
-    unsigned long long* run_ctr;
-    int* overflow;                   // set when a claim does not fit: hits are then rewritten directly
-    int qbase;                       // batch-global index of the request's first query
-};
-// Per-warp claim state, kept by the caller across chunks (lane 0's copy).
-struct StageCursor {
-    long long hit_next = 0, hit_end = 0;
-    long long run_next = 0, run_end = 0;
-};
-constexpr int STAGE_HIT_SEG = 512;  // hit slots per claim
-constexpr int STAGE_RUN_SEG = 128;  // run records per claim
-constexpr int RANGE_COUNT = 0, RANGE_WRITE = 1, RANGE_STAGE = 2;
-
-// Pads the rest of a warp's run segment with empty runs (call once, by lane 0,
-// when the warp is done).
-__device__ __forceinline__ void stage_close(const RangeStage& rs, StageCursor& cur) {
-    for (long long r = cur.run_next; r < cur.run_end && r < rs.run_cap; ++r) rs.runs[r] = make_int4(0, 0, 0, 0);
-    cur.run_next = cur.run_end;
-}
+constexpr int RANGE_COUNT = 0, RANGE_WRITE = 1;
 
 // MODE 0: box, MODE 1: radius.  OUT = RANGE_COUNT counts, RANGE_WRITE emits at
-// the query's CSR offset, RANGE_STAGE emits to a RangeStage.
+// the query's CSR offset.
 // Box (MODE 0) / radius (MODE 1) search of query qi by this thread, with the
 // leaves scanned by the whole warp.  Every lane of the warp calls this
 // together; lanes without a query pass valid = false.  "While-while": in the
@@ -400,8 +371,7 @@ template <int MODE, int OUT>
 __device__ __forceinline__ long long range_body(const DevTree& t, const float* __restrict__ q, int q_stride,
                                                 const float* __restrict__ radius, int r_stride, long long qi,
                                                 bool valid, long long o, long long o_lim, int* __restrict__ ids,
-                                                float* __restrict__ xyz, const RangeStage* rs = nullptr,
-                                                StageCursor* sc = nullptr) {
+                                                float* __restrict__ xyz) {
     constexpr bool WRITE = OUT != RANGE_COUNT;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -531,37 +501,6 @@ __device__ __forceinline__ long long range_body(const DevTree& t, const float* _
                     }
                 }
                 const unsigned hb = __ballot_sync(0xffffffffu, hit);
-                if (OUT == RANGE_STAGE && hb != 0) {
-                    // claim room for this step's hits and one run record
-                    const int nh = __popc(hb);
-                    long long hp = 0, rp = 0;
-                    if (lane == 0) {
-                        if (sc->hit_next + nh > sc->hit_end) {
-                            sc->hit_next = (long long)atomicAdd(rs->hit_ctr, (unsigned long long)STAGE_HIT_SEG);
-                            sc->hit_end = sc->hit_next + STAGE_HIT_SEG;
-                        }
-                        if (sc->run_next >= sc->run_end) {
-                            sc->run_next = (long long)atomicAdd(rs->run_ctr, (unsigned long long)STAGE_RUN_SEG);
-                            sc->run_end = sc->run_next + STAGE_RUN_SEG;
-                        }
-                        hp = sc->hit_next;
-                        rp = sc->run_next;
-                        sc->hit_next += nh;
-                        sc->run_next += 1;
-                    }
-                    hp = __shfl_sync(0xffffffffu, hp, 0);
-                    rp = __shfl_sync(0xffffffffu, rp, 0);
-                    const long long before = __shfl_sync(0xffffffffu, count, src[u]);
-                    const long long hq = __shfl_sync(0xffffffffu, qi, src[u]);
-                    if (hp + nh <= rs->hit_cap && rp < rs->run_cap) {
-                        if (hit)
-                            rs->hits[hp + __popc(hb & lt)] =
-                                make_float4(p[u].x, p[u].y, p[u].z, __uint_as_float(__float_as_uint(p[u].w) & ID_MASK));
-                        if (lane == 0) rs->runs[rp] = make_int4(rs->qbase + (int)hq, (int)hp, nh, (int)before);
-                    } else if (lane == 0) {
-                        atomicExch(rs->overflow, 1);
-                    }
-                }
                 if (OUT == RANGE_WRITE) {
                     const long long base = __shfl_sync(0xffffffffu, o + count, src[u]);
                     const long long lim = __shfl_sync(0xffffffffu, o_lim, src[u]);

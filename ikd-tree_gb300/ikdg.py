@@ -80,7 +80,7 @@ SIGNATURES = {
     "ikdg_batch_set_knn_lanes": (C.c_int, [_vp, C.c_int32, C.c_int32]),
     "ikdg_batch_set_graph": (C.c_int, [_vp, C.c_int]),
     "ikdg_batch_set_query_order": (C.c_int, [_vp, C.c_int]),
-    "ikdg_batch_set_range_staging": (C.c_int, [_vp, C.c_int, C.c_int64]),
+    "ikdg_batch_set_range_mode": (C.c_int, [_vp, C.c_int]),
     "ikdg_batch_run": (C.c_int, [_vp]),
     "ikdg_batch_synchronize": (C.c_int, [_vp, _lp]),
     "ikdg_batch_autotune": (C.c_int, [_vp, C.c_int32, _ip]),
@@ -480,11 +480,10 @@ class Batch:
     def set_graph(self, use_graph: bool):
         self._check(self.lib.ikdg_batch_set_graph(self.h, 1 if use_graph else 0), "batch_set_graph")
 
-    def set_range_staging(self, single_pass: bool, hit_capacity: int = 0):
-        """Box / radius requests in one walk with staged hits (default), or a
-        counting walk and a writing walk."""
-        self._check(self.lib.ikdg_batch_set_range_staging(self.h, 1 if single_pass else 0, int(hit_capacity)),
-                    "batch_set_range_staging")
+    def set_range_mode(self, fused: bool):
+        """Box / radius requests as one fused count-offset-write kernel
+        (default), or a counting walk, a prefix sum and a writing walk."""
+        self._check(self.lib.ikdg_batch_set_range_mode(self.h, 1 if fused else 0), "batch_set_range_mode")
 
     def set_query_order(self, ordered: bool):
         """Search every request's queries in spatial (Morton) order (default on)."""

@@ -227,16 +227,20 @@ def test_batch_query_order_changes_nothing(scene):
     assert_same(ordered, plain, reqs)
 
 
-def test_batch_range_passes_agree(scene):
-    """Range requests in one walk with staged hits, with a staging array too
-    small (the run falls back to the writing walk), and as a counting walk
-    plus a writing walk (the default): the same bytes as the per-call path."""
+def test_batch_range_modes_agree(scene):
+    """Range requests as one fused kernel (count, look-back offsets, write:
+    the default) and as a counting walk, a prefix sum and a writing walk,
+    with queries in Morton order and in the given order: the same bytes as
+    the per-call path."""
     maps, trees, empty, reqs, b = scene
     ref = per_call(reqs)
-    for single, cap in ((True, 0), (True, 1000), (False, 0)):
-        b.set_range_staging(single, cap)
-        assert_same(batched(b, reqs), ref, reqs)
-    b.set_range_staging(False, 0)
+    for fused in (True, False):
+        for ordered in (True, False):
+            b.set_range_mode(fused)
+            b.set_query_order(ordered)
+            assert_same(batched(b, reqs), ref, reqs)
+    b.set_range_mode(True)
+    b.set_query_order(True)
 
 
 def test_batch_range_requests_match_oracle(scene):
