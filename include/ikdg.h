@@ -192,12 +192,12 @@ int ikdg_batch_add_radius_search(ikdg_batch* b, ikdg_tree* t, const float* cente
 int ikdg_batch_set_knn_lanes(ikdg_batch* b, int32_t request, int32_t lanes);
 /* use_graph 0: issue the same kernels directly at every run (no graph). */
 int ikdg_batch_set_graph(ikdg_batch* b, int use_graph);
-/* ordered 1 (default): each run first sorts every request's queries by a
- * Morton code in its tree's box (one key pass and one radix sort for the
- * whole batch) and searches the kNN requests (and, with the range mode 0, the
- * box / radius requests) in that order, so neighbouring lanes walk nearby
- * nodes; results are unchanged and stay in query order.  0: queries are
- * searched in the order given. */
+/* ordered 1: each run first sorts every request's queries by a Morton code
+ * in its tree's box (one key pass and one radix sort for the whole batch) and
+ * searches the kNN requests (and, with the range mode 0, the box / radius
+ * requests) in that order, so neighbouring lanes walk nearby nodes; results
+ * are unchanged and stay in query order.  0 (default): queries are searched in
+ * the order given. */
 int ikdg_batch_set_query_order(ikdg_batch* b, int ordered);
 /* fused 1 (default): box / radius requests run in one kernel in which every
  * warp counts the hits of its 32 queries, takes their CSR offsets from the
