@@ -575,15 +575,23 @@ struct Tree {
             float4* ovf_pts = c.take<float4>(n);
             CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
             launch_pack_points(dt, raw, stride, n, next_id, packed, stream);
-            read_status();
-            if (st->err & ERR_INPUT) throw BadArg{"add_points: non-finite coordinate"};
-            next_id += n;
             if (st->root_code == 0) {
+                read_status();
+                if (st->err & ERR_INPUT) throw BadArg{"add_points: non-finite coordinate"};
+                next_id += n;
                 build_root(packed, n);
                 return;
             }
+            // no status read before the insertion: route_append_kernel does
+            // nothing once a non-finite input has set ERR_INPUT, and the read
+            // that ends finish_update reports it
             launch_route_append(dt, aux, packed, n, ovf_leaf, ovf_pts, stream);
+            next_id += n;  // taken even if a later step fails: ids are never reused
             finish_update(ovf_leaf, ovf_pts, (int)n);
+            if (st->err & ERR_INPUT) {
+                next_id -= n;  // nothing was inserted
+                throw BadArg{"add_points: non-finite coordinate"};
+            }
             return;
         }
         // Voxel downsampling.
@@ -598,36 +606,48 @@ struct Tree {
         carve_ds_scratch(op.p == nullptr ? nullptr : (char*)op.p + c.off, n, &d);
         CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
         launch_ds_prepare(dt, raw, stride, n, ds_size, d, stream);
-        read_status();
-        if (st->err & ERR_INPUT) throw BadArg{"add_points: non-finite coordinate"};
-        const int n_groups = st->n_groups;
+        // No status read between the phases of a sub-batch: the kernels read
+        // the group count, the sub-batch end and the non-finite flag on the
+        // device (n bounds the group count for their grids), and the status
+        // read that ends the sub-batch brings all three back.
+        const int n_bound = (int)n;
         const long long first_id = next_id;
+        next_id += n;  // taken even if a later step fails: ids are never reused
         long long a = 0;
         while (a < n) {
             launch_set_ll((long long*)((char*)st_dev + offsetof(DevStatus, count)), n, stream);
             if (debug_validate) check_valid("start of a downsampling sub-batch");
-            launch_ds_search(dt, n, ds_size, a, d, n_groups, stream);
-            read_status();
-            long long e = std::min<long long>(std::max<long long>(st->count, a + 1), n);
+            launch_ds_search(dt, n, ds_size, a, d, n_bound, stream);
             zero_fields(offsetof(DevStatus, n_ins), sizeof(int));
-            launch_ds_fold(dt, aux, n, a, e, first_id, d, n_groups, stream);
+            launch_ds_fold(dt, aux, n, a, first_id, d, n_bound, stream);
             if (debug_validate) {
                 read_status();
-                std::string m = "sub-batch [" + std::to_string(a) + "," + std::to_string(e) + ") groups " +
-                                std::to_string(n_groups) + " ins " + std::to_string(st->n_ins) + " items " +
-                                std::to_string(st->n_items);
+                std::string m = "sub-batch from " + std::to_string(a) + " to " + std::to_string(st->count) +
+                                " groups " + std::to_string(st->n_groups) + " ins " + std::to_string(st->n_ins) +
+                                " items " + std::to_string(st->n_items);
                 dbg_note = m;
             }
             if (st->root_code == 0) {
                 read_status();
+                if (st->err & ERR_INPUT) {
+                    next_id = first_id;  // nothing was inserted
+                    throw BadArg{"add_points: non-finite coordinate"};
+                }
                 if (st->n_ins > 0) build_root(d.ins, st->n_ins);
             } else {
-                launch_route_append_dev_count(dt, aux, d.ins, n_groups, &st_dev->n_ins, ovf_leaf, ovf_pts, stream);
-                finish_update(ovf_leaf, ovf_pts, n_groups);
+                launch_route_append_dev_count(dt, aux, d.ins, n_bound, &st_dev->n_ins, ovf_leaf, ovf_pts, stream);
+                finish_update(ovf_leaf, ovf_pts, n_bound);
+                // a non-finite input left the tree untouched (no kernel above
+                // changed anything once ERR_INPUT was set)
+                if (st->err & ERR_INPUT) {
+                    next_id = first_id;
+                    throw BadArg{"add_points: non-finite coordinate"};
+                }
             }
-            a = e;
+            // finish_update / build_root ended with a status read: st->count
+            // is the end ds_h1_kernel found for this sub-batch
+            a = std::min<long long>(std::max<long long>(st->count, a + 1), n);
         }
-        next_id += n;
         // Every sub-batch ended with a status read (finish_update, build_root
         // or the read before it), so count2 is current.
         if (n_added) *n_added = st->count2;

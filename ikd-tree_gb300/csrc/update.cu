@@ -50,6 +50,7 @@ __global__ void route_append_kernel(DevTree t, UpdateAux a, const float4* __rest
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long lim = n_dev != nullptr ? (long long)*n_dev : n;
     if (i >= lim) return;
+    if (t.st->err & ERR_INPUT) return;  // a non-finite input: the call changes nothing
     float4 p = pts[i];
     int code = __float_as_int(t.node[3].x);  // sentinel's left child = root
     if (code == 0) {
@@ -942,6 +943,7 @@ __global__ void ds_h1_kernel(long long n, long long a, DsScratch d, DevStatus* s
 __global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, long long a, DsScratch d, float ds) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= t.st->n_groups) return;
+    if (t.st->err & ERR_INPUT) return;  // a non-finite input: the call changes nothing
     int j = d.groups[g];
     long long first = group_first_from(d, n, j, a);
     if (first < 0) {
@@ -1015,10 +1017,14 @@ __global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, 
     }
 }
 
-__global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, long long a, long long e,
-                                                      long long first_id, DsScratch d) {
+__global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, long long a, long long first_id,
+                                                      DsScratch d) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= t.st->n_groups) return;
+    if (t.st->err & ERR_INPUT) return;  // a non-finite input: the call changes nothing
+    // the sub-batch ends where ds_h1_kernel found the first point that must
+    // be folded alone (st->count), and holds at least one point
+    const long long e = min(max((long long)t.st->count, a + 1), n);
     int j = d.groups[g];
     int4 info = d.g_info[g];
     d.g_out[g] = make_int4(0, 0, 0, 0);
@@ -1088,6 +1094,7 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
 __global__ void __launch_bounds__(128) ds_delete_kernel(DevTree t, UpdateAux a, DsScratch d) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= t.st->n_groups) return;
+    if (t.st->err & ERR_INPUT) return;
     if (!d.g_out[g].x) return;
     int lead = d.hval[0][d.groups[g]];
     float4 blo = d.box_lo[lead], bhi = d.box_hi[lead];
@@ -1327,10 +1334,10 @@ void launch_ds_search(const DevTree& t, long long n, float ds, long long a, DsSc
     if (max_groups > 0) ds_search_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, d, ds);
 }
 
-void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long long a, long long e, long long first_id,
+void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long long a, long long first_id,
                     DsScratch& d, int max_groups, cudaStream_t s) {
     if (max_groups <= 0) return;
-    ds_fold_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, e, first_id, d);
+    ds_fold_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, first_id, d);
     ds_delete_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, aux, d);
 }
 

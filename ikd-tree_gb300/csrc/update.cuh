@@ -98,16 +98,20 @@ struct DsScratch {
 };
 size_t ds_scratch_bytes(long long n);
 void carve_ds_scratch(void* base, long long n, DsScratch* d);
-// Prepares keys and groups (once per batch).  st->n_groups = group count.
+// Prepares keys and groups (once per batch).  st->n_groups = group count;
+// a non-finite input sets ERR_INPUT, after which the kernels below change
+// nothing.  The kernels read the group count and the sub-batch end on the
+// device: max_groups only sizes their grids (any bound on the group count).
 void launch_ds_prepare(const DevTree& t, const float* in, int stride, long long n, float ds, DsScratch& d,
                        cudaStream_t s);
 // S0 search for all groups and the hazard split of the sub-batch [a, n):
 // st->count = first index where the sub-batch must end.
 void launch_ds_search(const DevTree& t, long long n, float ds, long long a, DsScratch& d, int max_groups,
                       cudaStream_t s);
-// Folds [a, e) per group, deletes the S0 sets that must go, and queues the
+// Folds [a, e) per group, with e = min(max(st->count, a + 1), n) the end
+// launch_ds_search found, deletes the S0 sets that must go, and queues the
 // surviving winners in d.ins (st->n_ins = count); st->count2 += triggers.
-void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long long a, long long e, long long first_id,
+void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long long a, long long first_id,
                     DsScratch& d, int max_groups, cudaStream_t s);
 
 }  // namespace ikdg

@@ -288,3 +288,28 @@ def test_host_direct_and_staged_paths_agree(ikdg_mod, monkeypatch):
         b = staged.knn(q, k, md)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("downsample", [False, True])
+def test_non_finite_input_rejected_without_change(ikdg_mod, downsample):
+    """A batch with a non-finite coordinate is refused with IKDG_BAD_ARG and
+    leaves the tree as it was (valid set, size, and the ids of later
+    insertions)."""
+    rng = np.random.default_rng(55)
+    pts = rng.uniform(-5, 5, (5000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, 0.3), spec.SpecTree(0.3)
+    tree.Build(pts)
+    ref.Build(pts)
+    bad = rng.uniform(-5, 5, (300, 3)).astype(np.float32)
+    bad[123, 1] = np.nan
+    size0 = tree.size()
+    with pytest.raises(ikdg_mod.IkdgError) as e:
+        tree.Add_Points(bad, downsample)
+    assert e.value.status == ikdg_mod.BAD_ARG
+    assert tree.size() == size0
+    assert_same_valid(tree, ref)
+    good = rng.uniform(-5, 5, (300, 3)).astype(np.float32)
+    assert tree.Add_Points(good, downsample) == ref.Add_Points(good, downsample)
+    assert_same_valid(tree, ref)
+    assert tree.validate() == 0
+    tree.close()
