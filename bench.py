@@ -855,7 +855,34 @@ def run_leg(args):
     import torch
     import ikdg
     torch.cuda.set_device(0)
-    if args.leg == "lidar":
+    if args.leg == "knn":
+        # the headline step alone: `warmup` device steps (queries and results
+        # in HBM), then `steps` end-to-end steps (pinned host buffers, results
+        # written by the kernel)
+        tree = ikdg.KDTree(0.5, 0.6, DS)
+        tree.Build(make_map())
+        dev = torch.device("cuda", 0)
+        qh = make_queries(0)
+        q = torch.from_numpy(qh).to(dev)
+        ids = torch.empty((N_Q, K), dtype=torch.int32, device=dev)
+        d2 = torch.empty((N_Q, K), dtype=torch.float32, device=dev)
+        xyz = torch.empty((N_Q, K, 3), dtype=torch.float32, device=dev)
+        for _ in range(args.warmup):
+            tree.knn_device(q.data_ptr(), N_Q, K, math.inf, ids.data_ptr(), d2.data_ptr(), xyz.data_ptr())
+        tree.synchronize()
+        qp = torch.from_numpy(qh).pin_memory()
+        h = [torch.empty(sh, dtype=dt).pin_memory() for sh, dt in (((N_Q, K), torch.int32), ((N_Q, K), torch.float32),
+                                                                    ((N_Q, K, 3), torch.float32), ((N_Q,), torch.int32))]
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            tree.knn_into(qp.data_ptr(), N_Q, K, math.inf, *(x.data_ptr() for x in h))
+            ts.append(1e3 * (time.perf_counter() - t0))
+        same = bool((h[0].numpy() == ids.cpu().numpy()).all() and (h[1].numpy() == d2.cpu().numpy()).all())
+        out = {"e2e_ms": statistics.median(ts), "host_rows_equal_device_rows": same}
+        del qp, h
+        tree.close()
+    elif args.leg == "lidar":
         base, scans = lidar_workload()
         t = ikdg.KDTree(0.5, 0.6, DS)
         t.Build(base)
@@ -877,7 +904,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the multi-map batch leg")
     ap.add_argument("--no-stress", action="store_true", help="skip the 20M-point scale leg")
-    ap.add_argument("--leg", choices=["lidar", "batch", "stress"], default=None,
+    ap.add_argument("--leg", choices=["knn", "lidar", "batch", "stress"], default=None,
                     help="run one leg alone on GPU 0 (for profiling) and print its object")
     args = ap.parse_args()
     if args.leg is not None:
