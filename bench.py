@@ -427,9 +427,7 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
     b.set_query_order(True)
     batch_ordered_ms = timed(batched)
     b.set_query_order(False)
-    b.set_range_mode(False)
-    batch_two_pass_ms = timed(batched)
-    b.set_range_mode(True)
+
     batch_ms = timed(batched)
     batch_dev = batch_device_ms()
     tuned = None
@@ -458,9 +456,6 @@ def multimap_bench(ikdg, torch, device: int, reps: int = 5, tune: bool = True) -
         "batched_device_ms": batch_dev,
         "batched_ordered_ms": batch_ordered_ms,
         "batched_ordered": "the same batch with every kNN request's queries sorted by a Morton code first",
-        "batched_two_pass_ms": batch_two_pass_ms,
-        "batched_two_pass": "the same batch with box / radius requests as a counting walk, a prefix sum and a "
-                            "writing walk (the per-call scheme) instead of the fused kernel",
         "speedup_vs_plain": plain_ms / batch_ms,
         "speedup_vs_plain_sync": plain_sync_ms / batch_ms,
         "autotuned": tuned,

@@ -91,114 +91,6 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_search_kernel(const DevTr
     }
 }
 
-// Look-back states of a chunk's word: total not known yet, the chunk's own
-// total (aggregate), or the total of the request's chunks up to and including
-// it (inclusive).  The value sits above the two state bits.
-constexpr unsigned long long CS_EMPTY = 0, CS_AGG = 1, CS_INCL = 2;
-constexpr int LOOKBACK_SPINS = 1 << 20;
-
-__device__ __forceinline__ unsigned long long load_chunk_state(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.global.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void store_chunk_state(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.global.release.gpu.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// Range requests, fused: count, look back for the chunk's offset, write.
-template <int MODE>
-__device__ __forceinline__ void fused_range_chunk(const DevTree& t, const BatchReq& R, long long c, long long ci,
-                                                  long long c_begin, unsigned long long* __restrict__ cstat) {
-    const int lane = threadIdx.x & 31;
-    const long long qi = (c - R.c1) * BATCH_CHUNK + lane;
-    const bool valid = qi < R.nq;
-    const long long n = search::range_body<MODE, search::RANGE_COUNT>(t, R.q, R.q_stride, R.radius, R.r_stride, qi,
-                                                                     valid, 0, 0, nullptr, nullptr);
-    long long incl = n;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const long long v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += v;
-    }
-    const long long total = __shfl_sync(0xffffffffu, incl, 31);
-    long long prefix = 0;
-    if (lane == 0) {
-        if (c == R.c1) {
-            store_chunk_state(cstat + ci, ((unsigned long long)total << 2) | CS_INCL);
-        } else {
-            store_chunk_state(cstat + ci, ((unsigned long long)total << 2) | CS_AGG);
-            // every earlier chunk of the request was taken by a running warp
-            // and publishes its total right after its counting walk
-            long long p = ci - 1;
-            int spins = 0;
-            while (true) {
-                const unsigned long long w = load_chunk_state(cstat + p);
-                const unsigned long long st = w & 3ull;
-                if (st == CS_EMPTY) {
-                    if (++spins > LOOKBACK_SPINS) {
-                        atomicOr(&t.st->err, ERR_LOOP);
-                        prefix = -1;
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                prefix += (long long)(w >> 2);
-                if (st == CS_INCL || p + c_begin <= R.c1) break;
-                --p;
-            }
-            if (prefix >= 0) store_chunk_state(cstat + ci, ((unsigned long long)(prefix + total) << 2) | CS_INCL);
-        }
-    }
-    prefix = __shfl_sync(0xffffffffu, prefix, 0);
-    if (prefix < 0) return;  // gave up waiting (error raised): nothing written
-    const long long o = prefix + incl - n;
-    bool go = valid;
-    if (valid) {
-        R.offsets[qi] = o;
-        if (qi == R.nq - 1) {
-            R.offsets[R.nq] = o + n;
-            if (R.total != nullptr) *R.total = o + n;
-        }
-        if (n == 0 || R.ids == nullptr) {
-            go = false;
-        } else if (o + n > R.capacity) {
-            atomicOr(&t.st->err, ERR_OUTPUT);
-            go = false;
-        }
-    }
-    search::range_body<MODE, search::RANGE_WRITE>(t, R.q, R.q_stride, R.radius, R.r_stride, qi, go, o, o + n, R.ids,
-                                                  R.xyz);
-}
-
-__global__ void __launch_bounds__(BATCH_THREADS) batch_range_fused_kernel(const DevTree* __restrict__ trees,
-                                                                          const BatchReq* __restrict__ reqs,
-                                                                          const long long* __restrict__ req_c1,
-                                                                          int r0, int r1, long long c_begin,
-                                                                          long long c_end,
-                                                                          unsigned long long* __restrict__ ctr,
-                                                                          unsigned long long* __restrict__ cstat) {
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-        long long c = 0;
-        int r = -1;
-        if (lane == 0) {
-            c = c_begin + (long long)atomicAdd(ctr, 1ull);
-            r = c < c_end ? find_req(req_c1, r0, r1, c) : -1;
-        }
-        c = __shfl_sync(0xffffffffu, c, 0);
-        r = __shfl_sync(0xffffffffu, r, 0);
-        if (c >= c_end) break;
-        const BatchReq& R = reqs[r];
-        const DevTree t = trees[R.tree];
-        if (R.kind == BATCH_BOX)
-            fused_range_chunk<0>(t, R, c, c - c_begin, c_begin, cstat);
-        else
-            fused_range_chunk<1>(t, R, c, c - c_begin, c_begin, cstat);
-    }
-}
-
 // Phase 2: range requests write their CSR offsets and, where the request's
 // capacity holds the query's results, the ids / points.
 __global__ void __launch_bounds__(BATCH_THREADS) batch_write_kernel(const DevTree* __restrict__ trees,
@@ -375,20 +267,6 @@ void launch_batch_search(const DevTree* trees, const BatchReq* reqs, const long 
     const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
     const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
     search_dispatch(kclass, lanes, true, nullptr, trees, reqs, req_c1, r0, r1, c_begin, c_end, counts, ctr, g, s);
-}
-
-int batch_fused_grid() {
-    std::lock_guard<std::mutex> lock(g_grid_mu);
-    return resident_grid((const void*)batch_range_fused_kernel);
-}
-
-void launch_batch_range_fused(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
-                              long long c_begin, long long c_end, unsigned long long* ctr,
-                              unsigned long long* cstat, int grid, cudaStream_t s) {
-    if (c_end <= c_begin || r1 <= r0) return;
-    const long long ctas = (c_end - c_begin + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
-    const unsigned g = (unsigned)(ctas < grid ? ctas : grid);
-    batch_range_fused_kernel<<<g, BATCH_THREADS, 0, s>>>(trees, reqs, req_c1, r0, r1, c_begin, c_end, ctr, cstat);
 }
 
 void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long long* qstart, int n, long long total,

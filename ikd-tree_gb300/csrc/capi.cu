@@ -1188,12 +1188,6 @@ struct Batch {
     // query order.  Off by default: on 64 maps with 1.37M queries the sort
     // cost more than the coherence saved (8.08 ms against 7.85 ms).
     bool use_order = false;
-    // Range requests: 1 (default) one kernel in which each warp counts its
-    // chunk, takes its CSR offset by a look-back over the request's earlier
-    // chunks and writes at once, while the nodes and leaves it walked are
-    // still cached; 0: a counting walk over all range queries, one prefix sum,
-    // a writing walk (the per-call scheme).
-    int range_mode = 1;
     std::vector<Req> reqs;  // in the order added
     std::mutex mu;
     std::string err;
@@ -1225,11 +1219,6 @@ struct Batch {
     uint32_t* d_okeys[2] = {nullptr, nullptr};
     uint32_t* d_ovals[2] = {nullptr, nullptr};
     void* d_osort = nullptr;
-    // fused range requests (range_mode 1): per-chunk look-back words
-    bool fused = false;
-    unsigned long long* d_cstat = nullptr;
-    long long n_rchunks = 0, range_c_begin = 0;
-    int fused_grid = 0;
     DevStatus* d_st = nullptr;
     DevTree* h_trees = nullptr;      // pinned: read by the graph's first copy
     DevStatus* h_st = nullptr;       // pinned
@@ -1372,15 +1361,6 @@ struct Batch {
         c2_end = chunk2;
         for (auto& g : groups) g.grid = batch_search_grid(g.kclass, g.lanes);
         write_grid = batch_write_grid();
-        fused = range_mode == 1 && n_range_queries > 0;
-        n_rchunks = 0;
-        range_c_begin = 0;
-        for (auto& G : groups)
-            if (G.kclass == BATCH_RANGE_CLASS) {
-                if (n_rchunks == 0) range_c_begin = G.c_begin;
-                n_rchunks = G.c_end - range_c_begin;
-            }
-        if (fused) fused_grid = batch_fused_grid();
         // one allocation for the plan
         const size_t nt = trees.size(), nr = range_reqs.size();
         size_t bytes = align_up(sizeof(DevTree) * nt) + align_up(sizeof(BatchReq) * n) +
@@ -1391,7 +1371,6 @@ struct Batch {
         const long long nqo = ordered ? n_queries : 0;
         bytes += align_up(sizeof(long long) * (n + 1)) + 4 * align_up(sizeof(uint32_t) * std::max<long long>(nqo, 1)) +
                  align_up(ordered ? sort_temp_bytes(nqo, 1) : 0);
-        bytes += align_up(sizeof(unsigned long long) * std::max<long long>(n_rchunks, 1));
         CK(cudaMalloc(&dev, bytes));
         Carver c(dev);
         d_trees = c.take<DevTree>(nt);
@@ -1412,10 +1391,6 @@ struct Batch {
         }
         d_osort = ordered ? (void*)c.take<char>(sort_temp_bytes(nqo, 1)) : nullptr;
         for (int p = 0; p < n; ++p) d[p].perm = ordered ? (const int*)(d_ovals[0] + qstart[p]) : nullptr;
-        d_cstat = c.take<unsigned long long>(std::max<long long>(n_rchunks, 1));
-        if (fused)  // the look-back gives CSR offsets in query order: no permutation
-            for (int p = 0; p < n; ++p)
-                if (d[p].kind != BATCH_KNN) d[p].perm = nullptr;
         for (size_t j = 0; j < nr; ++j) d[pos_of[range_reqs[j]]].total = d_totals + j;
         CK(cudaMallocHost(&h_trees, sizeof(DevTree) * std::max<size_t>(nt, 1)));
         CK(cudaMemcpyAsync(d_reqs, d.data(), sizeof(BatchReq) * n, cudaMemcpyHostToDevice, stream));
@@ -1468,7 +1443,6 @@ struct Batch {
         CK(cudaMemcpyAsync(d_trees, h_trees, sizeof(DevTree) * trees.size(), cudaMemcpyHostToDevice, stream));
         CK(cudaMemsetAsync(d_ctr, 0, sizeof(unsigned long long) * 64, stream));
         CK(cudaMemsetAsync(d_st, 0, sizeof(DevStatus), stream));
-        if (fused) CK(cudaMemsetAsync(d_cstat, 0, sizeof(unsigned long long) * n_rchunks, stream));
         if (ordered) {
             launch_batch_keys(d_trees, d_reqs, d_qstart, (int)reqs.size(), n_queries, req_bits, d_okeys[0],
                               d_ovals[0], stream);
@@ -1480,16 +1454,12 @@ struct Batch {
             const Group& G = groups[g];
             cudaStream_t s = g == 0 ? stream : branch[g - 1];
             if (g > 0) CK(cudaStreamWaitEvent(s, ev_fork, 0));
-            if (fused && G.kclass == BATCH_RANGE_CLASS)
-                launch_batch_range_fused(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, d_ctr + g,
-                                         d_cstat + (G.c_begin - range_c_begin), fused_grid, s);
-            else
-                launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes,
-                                    d_counts, d_ctr + g, G.grid, s);
+            launch_batch_search(d_trees, d_reqs, d_c1, G.r0, G.r1, G.c_begin, G.c_end, G.kclass, G.lanes, d_counts,
+                                d_ctr + g, G.grid, s);
             if (g > 0) CK(cudaEventRecord(ev_join[g - 1], s));
         }
         for (size_t g = 1; g < groups.size(); ++g) CK(cudaStreamWaitEvent(stream, ev_join[g - 1], 0));
-        if (nridx > 0 && !fused) {
+        if (nridx > 0) {
             exclusive_scan(d_counts, d_goff, n_range_queries + 1, nullptr, d_scan, stream);
             launch_batch_write(d_trees, d_reqs, d_ridx, d_c2, nridx, c2_end, d_goff, d_ctr + 63, write_grid, stream);
         }
@@ -2146,12 +2116,6 @@ int ikdg_batch_set_query_order(ikdg_batch* h, int ordered) {
     });
 }
 
-int ikdg_batch_set_range_mode(ikdg_batch* h, int fused) {
-    return batch_guarded(h, [&](ikdg::Batch& b) {
-        b.drop_plan();
-        b.range_mode = fused != 0 ? 1 : 0;
-    });
-}
 
 int ikdg_batch_run(ikdg_batch* h) {
     return batch_guarded(h, [&](ikdg::Batch& b) { b.run(); });

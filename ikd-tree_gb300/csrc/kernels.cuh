@@ -145,17 +145,6 @@ void launch_batch_keys(const DevTree* trees, const BatchReq* reqs, const long lo
 // [0, c_end)); goff: exclusive scan of the batch count array.
 void launch_batch_write(const DevTree* trees, const BatchReq* reqs, const int* ridx, const long long* req_c2, int nr,
                         long long c_end, const long long* goff, unsigned long long* ctr, int grid, cudaStream_t s);
-// Range requests in one kernel: each warp counts its chunk's hits, takes the
-// chunk's CSR offset from the chunks of the same request before it (a
-// look-back over per-chunk totals: chunks are taken in order, so every chunk
-// it waits for belongs to a running warp) and writes its hits right away,
-// while the walked nodes and leaves are still in cache.  cstat: one zeroed
-// word per chunk of [c_begin, c_end).  Requests must run in query order (no
-// permutation).  A look-back that waits too long raises ERR_LOOP.
-int batch_fused_grid();
-void launch_batch_range_fused(const DevTree* trees, const BatchReq* reqs, const long long* req_c1, int r0, int r1,
-                              long long c_begin, long long c_end, unsigned long long* ctr,
-                              unsigned long long* cstat, int grid, cudaStream_t s);
 
 // ---- register.cu ---------------------------------------------------------------
 // Rt_dev: 12 doubles, R row-major then t.  planes: 2 float4 per point ({n,d}

@@ -80,7 +80,6 @@ SIGNATURES = {
     "ikdg_batch_set_knn_lanes": (C.c_int, [_vp, C.c_int32, C.c_int32]),
     "ikdg_batch_set_graph": (C.c_int, [_vp, C.c_int]),
     "ikdg_batch_set_query_order": (C.c_int, [_vp, C.c_int]),
-    "ikdg_batch_set_range_mode": (C.c_int, [_vp, C.c_int]),
     "ikdg_batch_run": (C.c_int, [_vp]),
     "ikdg_batch_synchronize": (C.c_int, [_vp, _lp]),
     "ikdg_batch_autotune": (C.c_int, [_vp, C.c_int32, _ip]),
@@ -479,11 +478,6 @@ class Batch:
 
     def set_graph(self, use_graph: bool):
         self._check(self.lib.ikdg_batch_set_graph(self.h, 1 if use_graph else 0), "batch_set_graph")
-
-    def set_range_mode(self, fused: bool):
-        """Box / radius requests as one fused count-offset-write kernel
-        (default), or a counting walk, a prefix sum and a writing walk."""
-        self._check(self.lib.ikdg_batch_set_range_mode(self.h, 1 if fused else 0), "batch_set_range_mode")
 
     def set_query_order(self, ordered: bool):
         """Search every request's queries in spatial (Morton) order (default on)."""

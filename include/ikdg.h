@@ -194,20 +194,10 @@ int ikdg_batch_set_knn_lanes(ikdg_batch* b, int32_t request, int32_t lanes);
 int ikdg_batch_set_graph(ikdg_batch* b, int use_graph);
 /* ordered 1: each run first sorts every request's queries by a Morton code
  * in its tree's box (one key pass and one radix sort for the whole batch) and
- * searches the kNN requests (and, with the range mode 0, the box / radius
- * requests) in that order, so neighbouring lanes walk nearby nodes; results
- * are unchanged and stay in query order.  0 (default): queries are searched in
+ * searches them in that order, so neighbouring lanes walk nearby nodes;
+ * results are unchanged and stay in query order.  0 (default): queries are searched in
  * the order given. */
 int ikdg_batch_set_query_order(ikdg_batch* b, int ordered);
-/* fused 1 (default): box / radius requests run in one kernel in which every
- * warp counts the hits of its 32 queries, takes their CSR offsets from the
- * totals of the request's earlier chunks (a look-back: chunks are handed out
- * in order, so every chunk a warp waits for belongs to a running warp) and
- * writes its hits at once, while the nodes and leaves it walked are still in
- * cache.  Range requests then run in query order.  0: a counting walk over
- * all range queries, one prefix sum and a writing walk, as the per-call path
- * does.  Results are the same. */
-int ikdg_batch_set_range_mode(ikdg_batch* b, int fused);
 /* Asynchronous on the batch's stream. */
 int ikdg_batch_run(ikdg_batch* b);
 /* Waits for the last run.  range_totals (nullable, host) receives one total

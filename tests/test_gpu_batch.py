@@ -217,30 +217,13 @@ def test_batch_knn_matches_oracle(scene):
 
 
 def test_batch_query_order_changes_nothing(scene):
-    """Searching every request's queries in Morton order (the default) and
-    in the given order gives the same bytes."""
-    maps, trees, empty, reqs, b = scene
-    ordered = batched(b, reqs)
-    b.set_query_order(False)
-    plain = batched(b, reqs)
-    b.set_query_order(True)
-    assert_same(ordered, plain, reqs)
-
-
-def test_batch_range_modes_agree(scene):
-    """Range requests as one fused kernel (count, look-back offsets, write:
-    the default) and as a counting walk, a prefix sum and a writing walk,
-    with queries in Morton order and in the given order: the same bytes as
-    the per-call path."""
+    """Every request's queries searched in Morton order and in the given
+    order (the default): the same bytes as the per-call path."""
     maps, trees, empty, reqs, b = scene
     ref = per_call(reqs)
-    for fused in (True, False):
-        for ordered in (True, False):
-            b.set_range_mode(fused)
-            b.set_query_order(ordered)
-            assert_same(batched(b, reqs), ref, reqs)
-    b.set_range_mode(True)
-    b.set_query_order(True)
+    for ordered in (True, False):
+        b.set_query_order(ordered)
+        assert_same(batched(b, reqs), ref, reqs)
 
 
 def test_batch_range_requests_match_oracle(scene):
