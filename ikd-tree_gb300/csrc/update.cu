@@ -150,8 +150,11 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         }
         // X's child codes do not change during a refit: read before arriving,
         // they let the last walker load the children's heights together with
-        // the record instead of after it.
+        // the record instead of after it;
         const float2 kids = __ldcg(reinterpret_cast<const float2*>(t.node + 4 * X + 3));
+        // so is X's parent link: loaded now, it is at hand when the last
+        // walker moves on instead of costing one more round trip per level
+        const int lp = __ldcg(&t.nparent[X]);
         // pend[X] is read before arriving: it cannot change until every
         // walker has arrived (the last one resets it), whereas after the
         // arrival the last walker may already have reset it to 0.
@@ -191,7 +194,6 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             a.viol_flag[X] = 1;
             list_push(t.st, &t.st->n_viol, a.viol, a.list_cap, X);
         }
-        int lp = t.nparent[X];
         int P = lp >> 1;
         write_child_box(t.node, P, lp & 1, b);
         write_child_cnt(t.ncnt, P, lp & 1, slots, del);
