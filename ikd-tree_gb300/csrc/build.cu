@@ -10,9 +10,10 @@
 // largest job:
 // * small (every job <= LB_SMALL points): one CTA per job builds the whole
 //   subtree in shared memory (local_build_kernel<LB_SMALL, 256>);
-// * medium (jobs <= MID_MAX): one CTA per job splits it down to LB_SMALL-point
-//   segments (mid_split_kernel: radix-selected median, stable partition), then
-//   the small local builder finishes them;
+// * medium (jobs <= MID_MAX): one launch per tree level splits every open
+//   segment of every job, one CTA per segment, down to LB_SMALL-point segments
+//   (mid_level_kernel: radix-selected median, stable partition), then the
+//   small local builder finishes them;
 // * large: each of the three coordinates is radix-sorted once; the three sorted
 //   index arrays are then stably partitioned level by level, so every segment
 //   stays a contiguous range in each array and its AABB is read off the ends of
@@ -570,10 +571,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
     }
 }
 
-// ---- CTA-per-job splitter for medium jobs -----------------------------------------
-// Jobs of up to MID_MAX points skip the global sort: one block per job splits
-// it level by level until every open segment fits the small local builder
-// (LB_SMALL points), whole segments at a time.  Per segment: the AABB by a block reduction of
+// ---- level-by-level splitter for medium jobs -------------------------------------------
+// Jobs of up to MID_MAX points skip the global sort: they are split one tree
+// level per launch until every open segment fits the small local builder
+// (LB_SMALL points), each open segment of a level by a block of its own (the
+// open segments of every job of the call share the launch).  Per segment: the AABB by a block reduction of
 // order-preserving keys; the median key on the longest axis by a four-pass
 // radix select (8-bit digits, shared histogram); then one stable partition
 // pass.  Keys below the median go left, keys equal to it go left in position
@@ -586,15 +588,12 @@ constexpr int MID_MAX = 1 << 17;
 constexpr int MID_THREADS = 1024;
 constexpr int MID_PPT = 4;
 constexpr int MID_TILE = MID_THREADS * MID_PPT;
-constexpr int MID_SEGS = 2 * (MID_MAX / LB_SMALL) + 2;  // open segments hold > LB_SMALL points each
 
 struct MidShared {
     int hist[256];
     uint32_t red[MID_THREADS / 32][6];
     uint32_t wsum[MID_THREADS / 32];
     uint32_t tot;
-    int4 seg[2][MID_SEGS];
-    int nseg[2];
     uint32_t box[6];
     int node, axis, digit, rank;
 };
@@ -630,218 +629,200 @@ __device__ __forceinline__ uint32_t mid_block_scan(uint32_t v, uint32_t* wsum, u
     return r;
 }
 
-__global__ void __launch_bounds__(MID_THREADS, 1) mid_split_kernel(DevTree t, const float4* pts,
-                                                                const int* __restrict__ job_off,
-                                                                const int* __restrict__ job_link, int njobs,
-                                                                float4* buf0, float4* buf1, uint32_t* keys,
+__global__ void __launch_bounds__(MID_THREADS, 1) mid_level_kernel(DevTree t, const float4* src, float4* dst,
+                                                                float4* buf0, uint32_t* keys,
+                                                                const int4* __restrict__ segs_in,
+                                                                const int* nseg_in, int4* __restrict__ segs_out,
+                                                                int* nseg_out, int max_segs,
                                                                 int4* __restrict__ local_jobs, int* nlocal,
                                                                 int max_local, int fill) {
     __shared__ MidShared sm;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int job = blockIdx.x; job < njobs; job += gridDim.x) {
-        if (tid == 0) {
-            sm.seg[0][0] = make_int4(job_off[job], job_off[job + 1], job_link[job], 0);
-            sm.nseg[0] = 1;
+    const int S = min(*nseg_in, max_segs);
+    for (int q = blockIdx.x; q < S; q += gridDim.x) {
+        const int4 sg = segs_in[q];
+        const int s = sg.x, e = sg.y, link = sg.z;
+        const int cnt = e - s;
+        __syncthreads();  // the previous segment's shared words are free again
+        if (cnt <= LB_SMALL) {  // only at level 0: a small job goes straight to the local builder
+            for (int i = s + tid; i < e; i += MID_THREADS) buf0[i] = src[i];
+            if (tid == 0) {
+                const int r = atomicAdd(nlocal, 1);
+                if (r < max_local) local_jobs[r] = make_int4(s, e, link, 0);
+                else atomicOr(&t.st->err, ERR_SEG);
+            }
+            continue;
+        }
+        // AABB.
+        uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+        for (int i = s + tid; i < e; i += MID_THREADS) {
+            const float4 p = src[i];
+            const uint32_t kx = float_key(p.x), ky = float_key(p.y), kz = float_key(p.z);
+            mn[0] = min(mn[0], kx), mx[0] = max(mx[0], kx);
+            mn[1] = min(mn[1], ky), mx[1] = max(mx[1], ky);
+            mn[2] = min(mn[2], kz), mx[2] = max(mx[2], kz);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = __reduce_min_sync(0xffffffffu, mn[a]);
+            mx[a] = __reduce_max_sync(0xffffffffu, mx[a]);
+        }
+        if (lane == 0)
+            for (int a = 0; a < 3; ++a) sm.red[warp][a] = mn[a], sm.red[warp][3 + a] = mx[a];
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                uint32_t lo = lane < MID_THREADS / 32 ? sm.red[lane][a] : 0xffffffffu;
+                uint32_t hi = lane < MID_THREADS / 32 ? sm.red[lane][3 + a] : 0u;
+                lo = __reduce_min_sync(0xffffffffu, lo);
+                hi = __reduce_max_sync(0xffffffffu, hi);
+                if (lane == 0) sm.box[a] = lo, sm.box[3 + a] = hi;
+            }
         }
         __syncthreads();
-        int cur = 0;
-        for (int level = 0; level < 32; ++level) {
-            const int S = sm.nseg[cur];
-            if (S == 0) break;
-            const float4* src = level == 0 ? pts : ((level & 1) ? buf0 : buf1);
-            float4* dst = (level & 1) ? buf1 : buf0;
-            if (tid == 0) sm.nseg[cur ^ 1] = 0;
-            for (int q = 0; q < S; ++q) {
-                const int4 sg = sm.seg[cur][q];
-                const int s = sg.x, e = sg.y, link = sg.z;
-                const int cnt = e - s;
-                __syncthreads();  // sm.seg / nseg reads done before they change
-                if (cnt <= LB_SMALL) {  // only at level 0: a small job goes straight to the local builder
-                    for (int i = s + tid; i < e; i += MID_THREADS) buf0[i] = src[i];
-                    if (tid == 0) {
-                        const int r = atomicAdd(nlocal, 1);
-                        if (r < max_local) local_jobs[r] = make_int4(s, e, link, 0);
-                        else atomicOr(&t.st->err, ERR_SEG);
+        // The node: axis, allocation, links into its parent.
+        if (tid == 0) {
+            Box3 b;
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = key_float(sm.box[a]);
+                b.hi[a] = key_float(sm.box[3 + a]);
+            }
+            float ext[3];
+            for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
+            int axis = 0;
+            if (ext[1] > ext[axis]) axis = 1;
+            if (ext[2] > ext[axis]) axis = 2;
+            const int X = alloc_node(t);
+            sm.node = X;
+            sm.axis = axis;
+            if (X >= 0) {
+                const int parent = link >> 1, side = link & 1;
+                t.nparent[X] = link;
+                int h = 0;
+                for (int m = cnt; m > fill; m -= m / 2) ++h;
+                t.nheight[X] = h;
+                write_child_box(t.node, parent, side, b);
+                write_child_code(t.node, parent, side, X);
+                write_child_cnt(t.ncnt, parent, side, cnt, 0);
+            }
+        }
+        __syncthreads();
+        const int X = sm.node, axis = sm.axis;
+        if (X < 0) continue;  // the pool is exhausted (flagged by alloc_node): the points are dropped
+        // Radix select of the key of rank m = cnt / 2.
+        const int m = cnt / 2;
+        uint32_t prefix = 0, pmask = 0;
+        int rank = m;
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = 24 - 8 * pass;
+            if (tid < 256) sm.hist[tid] = 0;
+            __syncthreads();
+            for (int base = s; base < e; base += MID_THREADS) {
+                const int i = base + tid;
+                bool ok = false;
+                uint32_t k = 0;
+                if (i < e) {
+                    if (pass == 0) {
+                        k = float_key(coord4(src[i], axis));
+                        keys[i] = k;
+                    } else {
+                        k = keys[i];
                     }
-                    continue;
+                    ok = (k & pmask) == prefix;
                 }
-                // AABB.
-                uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
-                for (int i = s + tid; i < e; i += MID_THREADS) {
-                    const float4 p = src[i];
-                    const uint32_t kx = float_key(p.x), ky = float_key(p.y), kz = float_key(p.z);
-                    mn[0] = min(mn[0], kx), mx[0] = max(mx[0], kx);
-                    mn[1] = min(mn[1], ky), mx[1] = max(mx[1], ky);
-                    mn[2] = min(mn[2], kz), mx[2] = max(mx[2], kz);
-                }
+                const int d = ok ? (int)((k >> shift) & 255u) : 256 + lane;
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                if (ok && lane == __ffs(peers) - 1) atomicAdd(&sm.hist[d], __popc(peers));
+            }
+            __syncthreads();
+            if (warp == 0) {
+                int c[8], sum = 0;
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    mn[a] = __reduce_min_sync(0xffffffffu, mn[a]);
-                    mx[a] = __reduce_max_sync(0xffffffffu, mx[a]);
-                }
-                if (lane == 0)
-                    for (int a = 0; a < 3; ++a) sm.red[warp][a] = mn[a], sm.red[warp][3 + a] = mx[a];
-                __syncthreads();
-                if (warp == 0) {
+                for (int j = 0; j < 8; ++j) c[j] = sm.hist[lane * 8 + j], sum += c[j];
+                int inc = sum;
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        uint32_t lo = lane < MID_THREADS / 32 ? sm.red[lane][a] : 0xffffffffu;
-                        uint32_t hi = lane < MID_THREADS / 32 ? sm.red[lane][3 + a] : 0u;
-                        lo = __reduce_min_sync(0xffffffffu, lo);
-                        hi = __reduce_max_sync(0xffffffffu, hi);
-                        if (lane == 0) sm.box[a] = lo, sm.box[3 + a] = hi;
-                    }
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
                 }
-                __syncthreads();
-                // The node: axis, allocation, links into its parent.
-                if (tid == 0) {
-                    Box3 b;
-                    for (int a = 0; a < 3; ++a) {
-                        b.lo[a] = key_float(sm.box[a]);
-                        b.hi[a] = key_float(sm.box[3 + a]);
-                    }
-                    float ext[3];
-                    for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
-                    int axis = 0;
-                    if (ext[1] > ext[axis]) axis = 1;
-                    if (ext[2] > ext[axis]) axis = 2;
-                    const int X = alloc_node(t);
-                    sm.node = X;
-                    sm.axis = axis;
-                    if (X >= 0) {
-                        const int parent = link >> 1, side = link & 1;
-                        t.nparent[X] = link;
-                        int h = 0;
-                        for (int m = cnt; m > fill; m -= m / 2) ++h;
-                        t.nheight[X] = h;
-                        write_child_box(t.node, parent, side, b);
-                        write_child_code(t.node, parent, side, X);
-                        write_child_cnt(t.ncnt, parent, side, cnt, 0);
-                    }
-                }
-                __syncthreads();
-                const int X = sm.node, axis = sm.axis;
-                if (X < 0) continue;  // the pool is exhausted (flagged by alloc_node): the points are dropped
-                // Radix select of the key of rank m = cnt / 2.
-                const int m = cnt / 2;
-                uint32_t prefix = 0, pmask = 0;
-                int rank = m;
-                for (int pass = 0; pass < 4; ++pass) {
-                    const int shift = 24 - 8 * pass;
-                    if (tid < 256) sm.hist[tid] = 0;
-                    __syncthreads();
-                    for (int base = s; base < e; base += MID_THREADS) {
-                        const int i = base + tid;
-                        bool ok = false;
-                        uint32_t k = 0;
-                        if (i < e) {
-                            if (pass == 0) {
-                                k = float_key(coord4(src[i], axis));
-                                keys[i] = k;
-                            } else {
-                                k = keys[i];
-                            }
-                            ok = (k & pmask) == prefix;
+                const int before = inc - sum;
+                if (rank >= before && rank < inc) {  // exactly one lane
+                    int r = rank - before, d = lane * 8;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (r < c[j]) {
+                            d = lane * 8 + j;
+                            break;
                         }
-                        const int d = ok ? (int)((k >> shift) & 255u) : 256 + lane;
-                        const unsigned peers = __match_any_sync(0xffffffffu, d);
-                        if (ok && lane == __ffs(peers) - 1) atomicAdd(&sm.hist[d], __popc(peers));
+                        r -= c[j];
                     }
-                    __syncthreads();
-                    if (warp == 0) {
-                        int c[8], sum = 0;
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) c[j] = sm.hist[lane * 8 + j], sum += c[j];
-                        int inc = sum;
-#pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
-                            const int y = __shfl_up_sync(0xffffffffu, inc, o);
-                            if (lane >= o) inc += y;
-                        }
-                        const int before = inc - sum;
-                        if (rank >= before && rank < inc) {  // exactly one lane
-                            int r = rank - before, d = lane * 8;
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                if (r < c[j]) {
-                                    d = lane * 8 + j;
-                                    break;
-                                }
-                                r -= c[j];
-                            }
-                            sm.digit = d;
-                            sm.rank = r;
-                        }
-                    }
-                    __syncthreads();
-                    prefix |= (uint32_t)sm.digit << shift;
-                    pmask |= 255u << shift;
-                    rank = sm.rank;
-                }
-                const uint32_t v = prefix;
-                const uint32_t need = (uint32_t)rank;  // keys equal to v that go left
-                if (tid == 0)
-                    t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0), key_float(v),
-                                                    __int_as_float(axis));
-                // Stable partition: left = keys below v, then the first `need`
-                // keys equal to v.  Packed counts: below v low, equal high.
-                uint32_t carry_lt = 0, carry_eq = 0;
-                for (int base = s; base < e; base += MID_TILE) {
-                    const int i0 = base + tid * MID_PPT;
-                    uint32_t kk[MID_PPT];
-                    uint32_t sum = 0;
-#pragma unroll
-                    for (int r = 0; r < MID_PPT; ++r) {
-                        const int i = i0 + r;
-                        kk[r] = i < e ? keys[i] : 0xffffffffu;
-                        if (i < e) sum += kk[r] < v ? 1u : (kk[r] == v ? 0x10000u : 0u);
-                    }
-                    uint32_t total;
-                    const uint32_t ex = mid_block_scan(sum, sm.wsum, &sm.tot, &total);
-                    uint32_t lt = carry_lt + (ex & 0xffffu), eq = carry_eq + (ex >> 16);
-#pragma unroll
-                    for (int r = 0; r < MID_PPT; ++r) {
-                        const int i = i0 + r;
-                        if (i >= e) break;
-                        const uint32_t k = kk[r];
-                        const bool left = k < v || (k == v && eq < need);
-                        const uint32_t lb = lt + (eq < need ? eq : need);
-                        const int dest = left ? s + (int)lb : s + m + (i - s - (int)lb);
-                        if (dest >= s && dest < e) dst[dest] = src[i];
-                        else atomicOr(&t.st->err, ERR_SEG);  // cannot happen: the select found rank m
-                        if (k < v) ++lt;
-                        else if (k == v) ++eq;
-                    }
-                    carry_lt += total & 0xffffu;
-                    carry_eq += total >> 16;
-                }
-                __syncthreads();  // the partition is complete before the children are read
-                // Children: small ones go to the local builder (from buffer 0),
-                // the others stay open.
-#pragma unroll 1
-                for (int c = 0; c < 2; ++c) {
-                    const int cs = c == 0 ? s : s + m, ce = c == 0 ? s + m : e;
-                    if (ce - cs <= LB_SMALL) {
-                        if (dst != buf0)
-                            for (int i = cs + tid; i < ce; i += MID_THREADS) buf0[i] = dst[i];
-                        if (tid == 0) {
-                            const int r = atomicAdd(nlocal, 1);
-                            if (r < max_local) local_jobs[r] = make_int4(cs, ce, X * 2 + c, 0);
-                            else atomicOr(&t.st->err, ERR_SEG);
-                        }
-                    } else if (tid == 0) {
-                        const int r = sm.nseg[cur ^ 1]++;
-                        if (r < MID_SEGS) sm.seg[cur ^ 1][r] = make_int4(cs, ce, X * 2 + c, 0);
-                        else atomicOr(&t.st->err, ERR_SEG);
-                    }
+                    sm.digit = d;
+                    sm.rank = r;
                 }
             }
             __syncthreads();
-            if (tid == 0 && sm.nseg[cur ^ 1] > MID_SEGS) sm.nseg[cur ^ 1] = MID_SEGS;
-            __syncthreads();
-            cur ^= 1;
+            prefix |= (uint32_t)sm.digit << shift;
+            pmask |= 255u << shift;
+            rank = sm.rank;
         }
-        __syncthreads();
+        const uint32_t v = prefix;
+        const uint32_t need = (uint32_t)rank;  // keys equal to v that go left
+        if (tid == 0)
+            t.node[4 * X + 3] = make_float4(__int_as_float(0), __int_as_float(0), key_float(v),
+                                            __int_as_float(axis));
+        // Stable partition: left = keys below v, then the first `need`
+        // keys equal to v.  Packed counts: below v low, equal high.
+        uint32_t carry_lt = 0, carry_eq = 0;
+        for (int base = s; base < e; base += MID_TILE) {
+            const int i0 = base + tid * MID_PPT;
+            uint32_t kk[MID_PPT];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int r = 0; r < MID_PPT; ++r) {
+                const int i = i0 + r;
+                kk[r] = i < e ? keys[i] : 0xffffffffu;
+                if (i < e) sum += kk[r] < v ? 1u : (kk[r] == v ? 0x10000u : 0u);
+            }
+            uint32_t total;
+            const uint32_t ex = mid_block_scan(sum, sm.wsum, &sm.tot, &total);
+            uint32_t lt = carry_lt + (ex & 0xffffu), eq = carry_eq + (ex >> 16);
+#pragma unroll
+            for (int r = 0; r < MID_PPT; ++r) {
+                const int i = i0 + r;
+                if (i >= e) break;
+                const uint32_t k = kk[r];
+                const bool left = k < v || (k == v && eq < need);
+                const uint32_t lb = lt + (eq < need ? eq : need);
+                const int dest = left ? s + (int)lb : s + m + (i - s - (int)lb);
+                if (dest >= s && dest < e) dst[dest] = src[i];
+                else atomicOr(&t.st->err, ERR_SEG);  // cannot happen: the select found rank m
+                if (k < v) ++lt;
+                else if (k == v) ++eq;
+            }
+            carry_lt += total & 0xffffu;
+            carry_eq += total >> 16;
+        }
+        __syncthreads();  // the partition is complete before the children are read
+        // Children: small ones go to the local builder (from buffer 0),
+        // the others stay open.
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {
+            const int cs = c == 0 ? s : s + m, ce = c == 0 ? s + m : e;
+            if (ce - cs <= LB_SMALL) {
+                if (dst != buf0)
+                    for (int i = cs + tid; i < ce; i += MID_THREADS) buf0[i] = dst[i];
+                if (tid == 0) {
+                    const int r = atomicAdd(nlocal, 1);
+                    if (r < max_local) local_jobs[r] = make_int4(cs, ce, X * 2 + c, 0);
+                    else atomicOr(&t.st->err, ERR_SEG);
+                }
+            } else if (tid == 0) {
+                const int r = atomicAdd(nseg_out, 1);
+                if (r < max_segs) segs_out[r] = make_int4(cs, ce, X * 2 + c, 0);
+                else atomicOr(&t.st->err, ERR_SEG);
+            }
+        }
     }
 }
 
@@ -970,11 +951,22 @@ void build_subtrees(const DevTree& t, const float4* pts, long long n, const int*
         return;
     }
     if (max_job <= MID_MAX) {
-        // Medium jobs: one block each splits down to the small builder's size.
+        // Medium jobs: one launch per level splits every open segment (one
+        // block each) until all of them fit the small local builder.
         reset_count_kernel<<<1, 1, 0, s>>>(bs.nseg + 2);
-        mid_split_kernel<<<grid(njobs, 1), MID_THREADS, 0, s>>>(t, pts, job_off, job_link, njobs, bs.mid_pts[0],
-                                                                 bs.mid_pts[1], (uint32_t*)bs.flag, bs.local_jobs,
-                                                                 bs.nseg + 2, (int)ms, fill);
+        init_segs_kernel<<<blocks_for(njobs, T), T, 0, s>>>(job_off, job_link, njobs, bs.segs[0], bs.nseg);
+        int levels = 0;
+        for (long long m = max_job; m > LB_SMALL; m -= m / 2) ++levels;
+        long long open = njobs;  // bound on the open segments of a level
+        for (int lv = 0; lv < std::max(levels, 1); ++lv) {
+            const float4* src = lv == 0 ? pts : ((lv & 1) ? bs.mid_pts[0] : bs.mid_pts[1]);
+            float4* dst = (lv & 1) ? bs.mid_pts[1] : bs.mid_pts[0];
+            reset_count_kernel<<<1, 1, 0, s>>>(bs.nseg + ((lv + 1) & 1));
+            mid_level_kernel<<<grid(std::min(open, ms), 1), MID_THREADS, 0, s>>>(
+                t, src, dst, bs.mid_pts[0], (uint32_t*)bs.flag, bs.segs[lv & 1], bs.nseg + (lv & 1),
+                bs.segs[(lv + 1) & 1], bs.nseg + ((lv + 1) & 1), (int)ms, bs.local_jobs, bs.nseg + 2, (int)ms, fill);
+            open = std::min(2 * open, ms);
+        }
         launch_local<LB_SMALL, 256>(grid(ms, 4), t, bs.mid_pts[0], nullptr, 0, nullptr, bs.local_jobs, bs.nseg + 2,
                                     (int)ms, fill, s);
         finish_alloc_kernel<<<1, 1, 0, s>>>(t.st);
