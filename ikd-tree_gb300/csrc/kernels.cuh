@@ -19,8 +19,10 @@ void exclusive_scan(const long long* in, long long* out, long long n, long long*
 // multiple of 8).  The result lands back in keys / vals; the *_alt buffers are
 // scratch of the same shape.  `temp` must hold sort_temp_bytes(n, batch).
 size_t sort_temp_bytes(long long n, int batch);
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, long long n,
-                      int batch, long long stride, int bits, void* temp, cudaStream_t s);
+// With copy_back = false an odd number of passes leaves the result in the
+// alt buffers, and the call returns true.
+bool radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, long long n,
+                      int batch, long long stride, int bits, void* temp, cudaStream_t s, bool copy_back = true);
 
 // ---- build.cu ---------------------------------------------------------------
 // Batched subtree build.  `pts` holds the points of `njobs` jobs back to back

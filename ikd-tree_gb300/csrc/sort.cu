@@ -14,9 +14,18 @@ constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;   // 4096
 
 constexpr int SORT_THREADS = 256;
-constexpr int SORT_ROUNDS = 16;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ROUNDS;  // 4096
+constexpr int SORT_MAX_ROUNDS = 16;
 constexpr int RADIX = 256;
+
+// Rounds of SORT_THREADS keys per tile: 16 for large sorts; small sorts (the
+// downsampling grouper's ~15k keys per scan) take smaller tiles, so that more
+// blocks share each pass while the histogram (tiles x RADIX x batch) still
+// fits the single-block scan.
+inline int sort_rounds(long long n, int batch) {
+    const long long per = (long long)SORT_MAX_ROUNDS * SORT_THREADS;
+    long long r = (n * batch + per - 1) / per;
+    return (int)(r < 1 ? 1 : r > SORT_MAX_ROUNDS ? SORT_MAX_ROUNDS : r);
+}
 
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v) {
@@ -152,13 +161,14 @@ void exclusive_scan_t(const T* in, T* out, long long n, T* total, void* temp, cu
 // ---- radix sort --------------------------------------------------------------
 
 __global__ void sort_hist_kernel(const uint32_t* __restrict__ keys, long long n, long long stride, int shift,
-                                 int ntiles, int* __restrict__ hist) {
+                                 int ntiles, int rounds, int* __restrict__ hist) {
     __shared__ int h[RADIX];
     for (int i = threadIdx.x; i < RADIX; i += SORT_THREADS) h[i] = 0;
     __syncthreads();
     const uint32_t* k = keys + (long long)blockIdx.y * stride;
-    long long base = (long long)blockIdx.x * SORT_TILE;
-    for (int i = threadIdx.x; i < SORT_TILE; i += SORT_THREADS) {
+    const int tile = rounds * SORT_THREADS;
+    long long base = (long long)blockIdx.x * tile;
+    for (int i = threadIdx.x; i < tile; i += SORT_THREADS) {
         long long g = base + i;
         if (g < n) atomicAdd(&h[(k[g] >> shift) & 0xff], 1);
     }
@@ -170,7 +180,8 @@ __global__ void sort_hist_kernel(const uint32_t* __restrict__ keys, long long n,
 
 __global__ void sort_scatter_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n,
-                                    long long stride, int shift, int ntiles, const int* __restrict__ offs) {
+                                    long long stride, int shift, int ntiles, int rounds,
+                                    const int* __restrict__ offs) {
     __shared__ int wcnt[SORT_THREADS / 32][RADIX];
     __shared__ int dbase[RADIX];
     const int b = blockIdx.y;
@@ -185,8 +196,8 @@ __global__ void sort_scatter_kernel(const uint32_t* __restrict__ keys, const uin
         dbase[d] = ob[(long long)d * ntiles + blockIdx.x] - (int)((long long)b * n);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
-    long long base = (long long)blockIdx.x * SORT_TILE;
-    for (int r = 0; r < SORT_ROUNDS; ++r) {
+    long long base = (long long)blockIdx.x * rounds * SORT_THREADS;
+    for (int r = 0; r < rounds; ++r) {
         for (int i = threadIdx.x; i < (SORT_THREADS / 32) * RADIX; i += SORT_THREADS) (&wcnt[0][0])[i] = 0;
         __syncthreads();
         long long g = base + (long long)r * SORT_THREADS + threadIdx.x;
@@ -237,15 +248,17 @@ void exclusive_scan(const long long* in, long long* out, long long n, long long*
 }
 
 size_t sort_temp_bytes(long long n, int batch) {
-    long long tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    const long long tile = (long long)sort_rounds(n, batch) * SORT_THREADS;
+    long long tiles = (n + tile - 1) / tile;
     long long hn = tiles * RADIX * batch;
     return (size_t)(hn * sizeof(int) * 2 + scan_temp_bytes(hn) + 512);
 }
 
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, long long n,
-                      int batch, long long stride, int bits, void* temp, cudaStream_t s) {
-    if (n <= 1 || batch <= 0) return;
-    int tiles = ceil_div_ll(n, SORT_TILE);
+bool radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, long long n,
+                      int batch, long long stride, int bits, void* temp, cudaStream_t s, bool copy_back) {
+    if (n <= 1 || batch <= 0) return false;
+    const int rounds = sort_rounds(n, batch);
+    int tiles = ceil_div_ll(n, (long long)rounds * SORT_THREADS);
     long long hn = (long long)tiles * RADIX * batch;
     int* hist = (int*)temp;
     int* offs = hist + hn;
@@ -255,17 +268,18 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32
     dim3 grid(tiles, batch);
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
-        sort_hist_kernel<<<grid, SORT_THREADS, 0, s>>>(ki, n, stride, shift, tiles, hist);
+        sort_hist_kernel<<<grid, SORT_THREADS, 0, s>>>(ki, n, stride, shift, tiles, rounds, hist);
         exclusive_scan(hist, offs, hn, nullptr, stemp, s);
-        sort_scatter_kernel<<<grid, SORT_THREADS, 0, s>>>(ki, vi, ko, vo, n, stride, shift, tiles, offs);
+        sort_scatter_kernel<<<grid, SORT_THREADS, 0, s>>>(ki, vi, ko, vo, n, stride, shift, tiles, rounds, offs);
         uint32_t* t;
         t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }
-    if (ki != keys) {
-        cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)((batch - 1) * stride + n), cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * (size_t)((batch - 1) * stride + n), cudaMemcpyDeviceToDevice, s);
-    }
+    if (ki == keys) return false;
+    if (!copy_back) return true;
+    cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * (size_t)((batch - 1) * stride + n), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * (size_t)((batch - 1) * stride + n), cudaMemcpyDeviceToDevice, s);
+    return false;
 }
 
 }  // namespace ikdg

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <utility>
 
 #include "update.cuh"
 
@@ -118,11 +119,25 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_items || i >= a.list_cap) return;
     int code = items[i];
+    // Per node X on the walk: its child codes, its parent link and its
+    // expected arrival count do not change during a refit (pend[X] is reset
+    // only by X's last walker, after every walker has arrived).  They are
+    // fetched one level ahead, in the same round trip as the level below's
+    // record, so each level costs the arrival and one load round trip.
+    auto invariants = [&](int X, float2& kids, int& lp, int& expect) {
+        kids = __ldcg(reinterpret_cast<const float2*>(t.node + 4 * X + 3));
+        lp = __ldcg(&t.nparent[X]);
+        expect = __ldcg(&a.pend[X]);
+    };
     int X;
+    float2 kids = make_float2(0.f, 0.f);
+    int lp = 0, expect = 0;
     if (code < 0) {
         int L = code_leaf(code);
-        int lp = t.lparent[L];
-        if (lp < 0) return;
+        int llp = t.lparent[L];
+        if (llp < 0) return;
+        X = llp >> 1;
+        if (X > 0) invariants(X, kids, lp, expect);
         int n = __ldcg(&t.leaf_n[L]);
         int m = n < LEAF_CAP ? n : LEAF_CAP;
         Box3 b = empty_box();
@@ -135,39 +150,32 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             else
                 box_grow(b, p.x, p.y, p.z);
         }
-        X = lp >> 1;
-        write_child_box(t.node, X, lp & 1, b);
-        write_child_cnt(t.ncnt, X, lp & 1, n, del);
+        write_child_box(t.node, X, llp & 1, b);
+        write_child_cnt(t.ncnt, X, llp & 1, n, del);
         if (n > LEAF_CAP)  // an overflowing bucket must be split
             list_push(t.st, &t.st->n_viol, a.viol, a.list_cap, code);
     } else {
         X = code;
+        if (X > 0) invariants(X, kids, lp, expect);
     }
     for (int steps = 0; X > 0; ++steps) {
         if (steps > MAX_WALK) {
             atomicOr(&t.st->err, ERR_LOOP);
             return;
         }
-        // X's child codes do not change during a refit: read before arriving,
-        // they let the last walker load the children's heights together with
-        // the record instead of after it;
-        const float2 kids = __ldcg(reinterpret_cast<const float2*>(t.node + 4 * X + 3));
-        // so is X's parent link: loaded now, it is at hand when the last
-        // walker moves on instead of costing one more round trip per level
-        const int lp = __ldcg(&t.nparent[X]);
-        // pend[X] is read before arriving: it cannot change until every
-        // walker has arrived (the last one resets it), whereas after the
-        // arrival the last walker may already have reset it to 0.
-        const int expect = __ldcg(&a.pend[X]);
         __threadfence();  // release: this walker's writes into X's record
         int old = atomicAdd(&a.arrive[X], 1);
         if (old + 1 < expect) return;
         __threadfence();  // acquire: the other children's writes are visible
         a.pend[X] = 0;
         a.arrive[X] = 0;
+        const int P = lp >> 1;
         const int hl = child_height(t, __float_as_int(kids.x)), hr = child_height(t, __float_as_int(kids.y));
         NodeRec r = load_node_cg(t.node, X);
         int4 cc = __ldcg(t.ncnt + X);
+        float2 kids_p = make_float2(0.f, 0.f);
+        int lp_p = 0, expect_p = 0;
+        if (P > 0) invariants(P, kids_p, lp_p, expect_p);
         Box3 b = empty_box();
         Box3 bl = r.box(0), br = r.box(1);
         if (!box_empty(bl)) box_union(b, bl);
@@ -194,10 +202,12 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             a.viol_flag[X] = 1;
             list_push(t.st, &t.st->n_viol, a.viol, a.list_cap, X);
         }
-        int P = lp >> 1;
         write_child_box(t.node, P, lp & 1, b);
         write_child_cnt(t.ncnt, P, lp & 1, slots, del);
         X = P;
+        kids = kids_p;
+        lp = lp_p;
+        expect = expect_p;
     }
 }
 
@@ -856,6 +866,10 @@ __global__ void snapshot_root_kernel(DevTree t) {
 // winner that was already in the map is re-inserted under its own id; a new
 // point i of the batch gets id first_id + i.
 
+// Bits of the voxel hash the grouper sorts by (and compares: entries of one
+// hash run are the sorted neighbours with equal masked hash).
+constexpr int DS_HASH_BITS = 24;
+
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     h ^= h >> 16;
     h *= 0x85ebca6bu;
@@ -904,34 +918,74 @@ __global__ void ds_prepare_kernel(DevTree t, const float* __restrict__ in, int s
     int kb[3];
     for (int a = 0; a < 3; ++a) kb[a] = __float_as_int(__fadd_rn(f[a], 0.0f));
     d.key[i] = make_int4(kb[0], kb[1], kb[2], clean ? 1 : 0);
-    uint32_t h = (uint32_t)kb[0] * 73856093u ^ (uint32_t)kb[1] * 19349663u ^ (uint32_t)kb[2] * 83492791u;
-    d.hkey[0][i] = mix32(h);
+    // The bit patterns of integral floats end in long runs of zeros: each
+    // component goes through the full mixer (a product of them kept only
+    // ~16 bits and put up to 7 voxels on one hash).
+    uint32_t h = mix32((uint32_t)kb[2] ^ 0x9e3779b9u);
+    h = mix32(h ^ (uint32_t)kb[1]);
+    d.hkey[0][i] = mix32(h ^ (uint32_t)kb[0]) & ((1u << DS_HASH_BITS) - 1u);
     d.hval[0][i] = (uint32_t)i;
 }
 
 __device__ __forceinline__ bool same_key(const int4& a, const int4& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
+// Also lays the keys and points out in sorted order (s_key, s_pts), so the
+// per-group walks below read consecutive entries instead of gathering through
+// hval one dependent load at a time.
 __global__ void ds_leaders_kernel(long long n, DsScratch d, DevStatus* st) {
     long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t h = d.hkey[0][j];
-    int4 k = d.key[d.hval[0][j]];
+    const uint32_t idx = d.hval[0][j];
+    int4 k = d.key[idx];
+    const float4 p = d.pts[idx];
+    d.s_key[j] = k;
+    d.s_pts[j] = make_float4(p.x, p.y, p.z, __int_as_float((int)idx));
     for (long long jj = j - 1; jj >= 0 && d.hkey[0][jj] == h; --jj)
         if (same_key(d.key[d.hval[0][jj]], k)) return;
     int g = atomicAdd(&st->n_groups, 1);
     d.groups[g] = (int)j;
 }
 
+// Entries of the hash run starting at sorted position j, four per step
+// (independent loads); f(jj, key, point) sees them in sorted order, which
+// within one voxel is input order, and returns false to stop.
+template <class F>
+__device__ __forceinline__ void for_run(const DsScratch& d, long long n, long long j, uint32_t h, F f) {
+    for (long long base = j; base < n; base += 4) {
+        uint32_t hh[4];
+        int4 kk[4];
+        float4 pp[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long jj = base + u;
+            hh[u] = jj < n ? __ldg(d.hkey[0] + jj) : ~h;
+            kk[u] = jj < n ? __ldg(d.s_key + jj) : make_int4(0, 0, 0, 0);
+            pp[u] = jj < n ? __ldg(d.s_pts + jj) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (hh[u] != h) return;
+            if (!f(base + u, kk[u], pp[u])) return;
+        }
+    }
+}
+
 // First member index >= a of group g (members are in increasing index order).
 __device__ __forceinline__ long long group_first_from(const DsScratch& d, long long n, int j, long long a) {
-    uint32_t h = d.hkey[0][j];
-    int4 k = d.key[d.hval[0][j]];
-    for (long long jj = j; jj < n && d.hkey[0][jj] == h; ++jj) {
-        uint32_t idx = d.hval[0][jj];
-        if (!same_key(d.key[idx], k)) continue;
-        if ((long long)idx >= a) return idx;
-    }
-    return -1;
+    const uint32_t h = __ldg(d.hkey[0] + j);
+    const int4 k = __ldg(d.s_key + j);
+    long long r = -1;
+    for_run(d, n, j, h, [&](long long, const int4& kk, const float4& p) {
+        if (!same_key(kk, k)) return true;
+        const long long idx = __float_as_int(p.w);
+        if (idx >= a) {
+            r = idx;
+            return false;
+        }
+        return true;
+    });
+    return r;
 }
 
 __global__ void ds_h1_kernel(long long n, long long a, DsScratch d, DevStatus* st) {
@@ -942,75 +996,174 @@ __global__ void ds_h1_kernel(long long n, long long a, DsScratch d, DevStatus* s
     atomicMin((long long*)&st->count, cut);
 }
 
-__global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, long long a, DsScratch d, float ds) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= t.st->n_groups) return;
-    if (t.st->err & ERR_INPUT) return;  // a non-finite input: the call changes nothing
-    int j = d.groups[g];
-    long long first = group_first_from(d, n, j, a);
-    if (first < 0) {
-        d.g_info[g] = make_int4(0, -1, 0, 0);
-        return;
+// Warp-collective walk of every lane's box (half-open, {lo, hi}) down the
+// tree: a node phase steps each lane through its own nodes until it holds a
+// leaf, then the warp scans the held leaves together, one lane per slot (one
+// coalesced 512-byte load per leaf).  For every held leaf every lane calls
+// leaf(src, L, p, nl): src = the lane holding leaf L, p = slot `lane` of L,
+// nl = L's fill count.  Every lane of the warp must call it; lanes without a
+// box pass active = false.  Slots are read with plain loads: ds_delete_kernel
+// flags slots of the leaves it walks.
+template <class F>
+__device__ __forceinline__ void warp_box_walk(const DevTree& t, bool active, const Box3& qb, F leaf) {
+    const int lane = threadIdx.x & 31;
+    int stack[MAX_STACK];
+    int sp = 0;
+    int cur = 0;  // node code (0 = the sentinel record, where the walk starts) or leaf code (< 0)
+    bool done = !active;
+    int visits = 0;
+    auto pop = [&]() {
+        if (sp > 0)
+            cur = stack[--sp];
+        else
+            done = true;
+    };
+    while (true) {
+        while (true) {
+            const bool nodework = !done && cur >= 0;
+            if (!__any_sync(0xffffffffu, nodework)) break;
+            if (!nodework) continue;
+            if (++visits > MAX_VISITS) {
+                atomicOr(&t.st->err, ERR_LOOP);
+                done = true;
+                continue;
+            }
+            const NodeRec r = load_node(t.node, cur);
+            int next = 0;
+            bool have_next = false;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int c = side == 0 ? r.left() : r.right();
+                if (c == 0) continue;
+                const Box3 b = r.box(side);
+                if (box_empty(b) || qbox_disjoint(qb, b)) continue;
+                if (!have_next) {
+                    next = c;
+                    have_next = true;
+                } else if (sp < MAX_STACK) {
+                    stack[sp++] = c;
+                } else {
+                    atomicOr(&t.st->err, ERR_STACK);
+                }
+            }
+            if (have_next)
+                cur = next;
+            else
+                pop();
+        }
+        const bool leafwork = !done && cur < 0;
+        unsigned lb = __ballot_sync(0xffffffffu, leafwork);
+        if (lb == 0) break;
+        while (lb) {
+            // two held leaves per step: their slot loads go out together
+            const int s0 = __ffs(lb) - 1;
+            lb &= lb - 1;
+            const int s1 = lb ? __ffs(lb) - 1 : -1;
+            if (lb) lb &= lb - 1;
+            const int L0 = code_leaf(__shfl_sync(0xffffffffu, cur, s0));
+            const int L1 = code_leaf(__shfl_sync(0xffffffffu, cur, s1 < 0 ? s0 : s1));
+            const float4 p0 = t.pts[(long long)L0 * LEAF_CAP + lane];
+            const int n0 = __ldg(t.leaf_n + L0);
+            float4 p1 = p0;
+            int n1 = 0;
+            if (s1 >= 0) {
+                p1 = t.pts[(long long)L1 * LEAF_CAP + lane];
+                n1 = __ldg(t.leaf_n + L1);
+            }
+            leaf(s0, L0, p0, min(n0, LEAF_CAP));
+            if (s1 >= 0) leaf(s1, L1, p1, min(n1, LEAF_CAP));
+        }
+        if (leafwork) pop();
     }
-    int lead = d.hval[0][j];
-    float4 blo = d.box_lo[lead], bhi = d.box_hi[lead], mid = d.mid[lead];
+}
+
+__device__ __forceinline__ Box3 group_box(const DsScratch& d, int lead) {
+    const float4 blo = d.box_lo[lead], bhi = d.box_hi[lead];
     Box3 qb;
     qb.lo[0] = blo.x; qb.lo[1] = blo.y; qb.lo[2] = blo.z;
     qb.hi[0] = bhi.x; qb.hi[1] = bhi.y; qb.hi[2] = bhi.z;
-    const float fk[3] = {blo.w, bhi.w, mid.w};
+    return qb;
+}
+
+__device__ __forceinline__ Box3 shfl_box(const Box3& b, int src) {
+    Box3 o;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        o.lo[k] = __shfl_sync(0xffffffffu, b.lo[k], src);
+        o.hi[k] = __shfl_sync(0xffffffffu, b.hi[k], src);
+    }
+    return o;
+}
+
+// Per voxel group: S = the valid stored points in the voxel's box, |S|, the
+// point of S closest to the voxel centre (smaller id on ties), and whether a
+// point of S also lies in a neighbouring voxel's box range on some axis (a
+// float-rounding sliver: the group is then folded alone).
+__global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, long long a, DsScratch d, float ds) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = g < t.st->n_groups && !(t.st->err & ERR_INPUT);  // a non-finite input: the call changes nothing
+    long long first = -1;
+    int lead = 0;
+    if (active) {
+        const int j = d.groups[g];
+        first = group_first_from(d, n, j, a);
+        if (first < 0) {
+            d.g_info[g] = make_int4(0, -1, 0, 0);
+            active = false;
+        } else {
+            lead = d.hval[0][j];
+        }
+    }
+    const Box3 qb = active ? group_box(d, lead) : empty_box();
+    const float4 mid = active ? d.mid[lead] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float fk0 = active ? d.box_lo[lead].w : 0.f, fk1 = active ? d.box_hi[lead].w : 0.f;
     int n0 = 0, best_slot = -1, best_id = 0x7fffffff;
     float best_d = __int_as_float(0x7f800000);
     float4 best_p = make_float4(0.f, 0.f, 0.f, 0.f);
     bool hazard = false;
-    int stack[MAX_STACK];
-    int sp = 0;
-    stack[sp++] = 0;
-    bool start = true;
-    int visits = 0;
-    while (sp > 0) {
-        if (++visits > MAX_VISITS) {
-            atomicOr(&t.st->err, ERR_LOOP);
-            break;
+    warp_box_walk(t, active, qb, [&](int src, int L, const float4& p, int nl) {
+        const Box3 hb = shfl_box(qb, src);
+        const uint32_t w = __float_as_uint(p.w);
+        const bool in = lane < nl && !(w & F_DEL) && qbox_holds(hb, p.x, p.y, p.z);
+        const unsigned inb = __ballot_sync(0xffffffffu, in);
+        if (inb == 0) return;
+        const float mx = __shfl_sync(0xffffffffu, mid.x, src), my = __shfl_sync(0xffffffffu, mid.y, src),
+                    mz = __shfl_sync(0xffffffffu, mid.z, src);
+        const float f0 = __shfl_sync(0xffffffffu, fk0, src), f1 = __shfl_sync(0xffffffffu, fk1, src),
+                    f2 = __shfl_sync(0xffffffffu, mid.w, src);
+        bool hz = false;
+        if (in) {
+            const float pc[3] = {p.x, p.y, p.z};
+            const float fk[3] = {f0, f1, f2};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (in_voxel_range(pc[k], fk[k], -1.f, ds) || in_voxel_range(pc[k], fk[k], 1.f, ds)) hz = true;
         }
-        int code = stack[--sp];
-        if (start || code > 0) {
-            start = false;
-            NodeRec r = load_node(t.node, code);
-            for (int side = 0; side < 2; ++side) {
-                int c = side == 0 ? r.left() : r.right();
-                if (c == 0) continue;
-                Box3 b = r.box(side);
-                if (box_empty(b) || qbox_disjoint(qb, b)) continue;
-                if (sp < MAX_STACK)
-                    stack[sp++] = c;
-                else
-                    atomicOr(&t.st->err, ERR_STACK);
-            }
-        } else {
-            int L = code_leaf(code);
-            int nl = t.leaf_n[L];
-            int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
-            const float4* lp = t.pts + (long long)L * LEAF_CAP;
-            for (int s = 0; s < ml; ++s) {
-                float4 p = __ldg(lp + s);
-                uint32_t w = __float_as_uint(p.w);
-                if (w & F_DEL) continue;
-                if (!qbox_holds(qb, p.x, p.y, p.z)) continue;
-                ++n0;
-                float dd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
-                int id = (int)(w & ID_MASK);
-                if (dd < best_d || (dd == best_d && id < best_id)) {
-                    best_d = dd;
-                    best_id = id;
-                    best_slot = L * LEAF_CAP + s;
-                    best_p = p;
-                }
-                const float pc[3] = {p.x, p.y, p.z};
-                for (int k = 0; k < 3; ++k)
-                    if (in_voxel_range(pc[k], fk[k], -1.f, ds) || in_voxel_range(pc[k], fk[k], 1.f, ds)) hazard = true;
+        const unsigned hzb = __ballot_sync(0xffffffffu, hz);
+        // (distance, id) minimum over the hits: squared distances are >= 0, so
+        // their bit patterns order like the values
+        const float dd = in ? sq_dist(p.x, p.y, p.z, mx, my, mz) : __int_as_float(0x7f800000);
+        const unsigned db = __float_as_uint(dd);
+        const unsigned dmin = __reduce_min_sync(0xffffffffu, db);
+        const unsigned id = in ? (w & ID_MASK) : 0xffffffffu;
+        const unsigned imin = __reduce_min_sync(0xffffffffu, db == dmin ? id : 0xffffffffu);
+        const int wl = __ffs(__ballot_sync(0xffffffffu, in && db == dmin && id == imin)) - 1;
+        const float bx = __shfl_sync(0xffffffffu, p.x, wl), by = __shfl_sync(0xffffffffu, p.y, wl),
+                    bz = __shfl_sync(0xffffffffu, p.z, wl);
+        if (lane == src) {
+            n0 += __popc(inb);
+            hazard = hazard || hzb != 0;
+            const float d0 = __uint_as_float(dmin);
+            if (d0 < best_d || (d0 == best_d && (int)imin < best_id)) {
+                best_d = d0;
+                best_id = (int)imin;
+                best_slot = L * LEAF_CAP + wl;
+                best_p = make_float4(bx, by, bz, 0.f);
             }
         }
-    }
+    });
+    if (!active) return;
     d.g_info[g] = make_int4(n0, best_slot, best_id, hazard ? 1 : 0);
     d.g_best[g] = make_float4(best_p.x, best_p.y, best_p.z, best_d);
     if (hazard) {
@@ -1031,9 +1184,9 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
     int4 info = d.g_info[g];
     d.g_out[g] = make_int4(0, 0, 0, 0);
     if (info.y == -1 && info.x == 0 && group_first_from(d, n, j, a) < 0) return;
-    uint32_t h = d.hkey[0][j];
-    int lead = d.hval[0][j];
-    int4 k = d.key[lead];
+    const uint32_t h = __ldg(d.hkey[0] + j);
+    const int lead = d.hval[0][j];
+    const int4 k = __ldg(d.s_key + j);
     float4 mid = d.mid[lead];
     float4 best = d.g_best[g];
     const int n0 = info.x;
@@ -1043,11 +1196,11 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
     int ins_old_id = -1;  // the winner is an existing point: it keeps its id
     int cw_old = -1;
     int triggers = 0;
-    for (long long jj = j; jj < n && d.hkey[0][jj] == h; ++jj) {
-        uint32_t idx = d.hval[0][jj];
-        if (!same_key(d.key[idx], k)) continue;
-        if ((long long)idx < a || (long long)idx >= e) continue;
-        float4 p = d.pts[idx];
+    for_run(d, n, j, h, [&](long long, const int4& kk, const float4& p) {
+        if (!same_key(kk, k)) return true;
+        const long long idx = __float_as_int(p.w);
+        if (idx < a) return true;
+        if (idx >= e) return false;  // members come in increasing index order
         float pd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
         float wx = p.x, wy = p.y, wz = p.z, wd = pd;
         int w_old = -1;
@@ -1077,7 +1230,8 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
             ins_idx = idx;
             ins_old_id = w_old;
         }
-    }
+        return true;
+    });
     d.g_out[g] = make_int4(del_s0 ? 1 : 0, have_ins ? 1 : 0, triggers, 0);
     if (triggers) atomicAdd((unsigned long long*)&t.st->count2, (unsigned long long)triggers);
     if (have_ins) {
@@ -1094,56 +1248,18 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
 // Deletes (with the downsample flag) every valid point in the boxes of the
 // groups whose fold decided so.
 __global__ void __launch_bounds__(128) ds_delete_kernel(DevTree t, UpdateAux a, DsScratch d) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= t.st->n_groups) return;
-    if (t.st->err & ERR_INPUT) return;
-    if (!d.g_out[g].x) return;
-    int lead = d.hval[0][d.groups[g]];
-    float4 blo = d.box_lo[lead], bhi = d.box_hi[lead];
-    Box3 qb;
-    qb.lo[0] = blo.x; qb.lo[1] = blo.y; qb.lo[2] = blo.z;
-    qb.hi[0] = bhi.x; qb.hi[1] = bhi.y; qb.hi[2] = bhi.z;
-    int stack[MAX_STACK];
-    int sp = 0;
-    stack[sp++] = 0;
-    bool start = true;
-    int visits = 0;
-    while (sp > 0) {
-        if (++visits > MAX_VISITS) {
-            atomicOr(&t.st->err, ERR_LOOP);
-            break;
-        }
-        int code = stack[--sp];
-        if (start || code > 0) {
-            start = false;
-            NodeRec r = load_node(t.node, code);
-            for (int side = 0; side < 2; ++side) {
-                int c = side == 0 ? r.left() : r.right();
-                if (c == 0) continue;
-                Box3 b = r.box(side);
-                if (box_empty(b) || qbox_disjoint(qb, b)) continue;
-                if (sp < MAX_STACK)
-                    stack[sp++] = c;
-                else
-                    atomicOr(&t.st->err, ERR_STACK);
-            }
-        } else {
-            int L = code_leaf(code);
-            int nl = t.leaf_n[L];
-            int ml = nl < LEAF_CAP ? nl : LEAF_CAP;
-            float4* lp = t.pts + (long long)L * LEAF_CAP;
-            bool any = false;
-            for (int s = 0; s < ml; ++s) {
-                float4 p = lp[s];
-                uint32_t w = __float_as_uint(p.w);
-                if (w & F_DEL) continue;
-                if (!qbox_holds(qb, p.x, p.y, p.z)) continue;
-                lp[s].w = __uint_as_float(w | F_DEL | F_DSDEL);
-                any = true;
-            }
-            if (any) mark_dirty(a, t.st, L);
-        }
-    }
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool active = g < t.st->n_groups && !(t.st->err & ERR_INPUT) && d.g_out[g].x;
+    const Box3 qb = active ? group_box(d, d.hval[0][d.groups[g]]) : empty_box();
+    warp_box_walk(t, active, qb, [&](int src, int L, const float4& p, int nl) {
+        const Box3 hb = shfl_box(qb, src);
+        const uint32_t w = __float_as_uint(p.w);
+        const bool in = lane < nl && !(w & F_DEL) && qbox_holds(hb, p.x, p.y, p.z);
+        if (in) t.pts[(long long)L * LEAF_CAP + lane].w = __uint_as_float(w | F_DEL | F_DSDEL);
+        const unsigned inb = __ballot_sync(0xffffffffu, in);
+        if (inb != 0 && lane == src) mark_dirty(a, t.st, L);
+    });
 }
 
 __global__ void pack_points_kernel(DevTree t, const float* __restrict__ in, int stride, long long n, long long first_id,
@@ -1289,7 +1405,8 @@ void launch_check_finite(const DevTree& t, const float* in, long long count, cud
 size_t ds_scratch_bytes(long long n) {
     size_t b = 0;
     b += 5 * au(sizeof(float4) * n);   // pts, box_lo, box_hi, mid, ins
-    b += au(sizeof(int4) * n);         // key
+    b += 2 * au(sizeof(int4) * n);     // key, s_key
+    b += au(sizeof(float4) * n);       // s_pts
     b += 4 * au(sizeof(uint32_t) * n); // hkey x2, hval x2
     b += au(sizeof(int) * n);          // groups
     b += 2 * au(sizeof(int4) * n);     // g_info, g_out
@@ -1311,6 +1428,8 @@ void carve_ds_scratch(void* base, long long n, DsScratch* d) {
     d->mid = (float4*)take(sizeof(float4) * n);
     d->ins = (float4*)take(sizeof(float4) * n);
     d->key = (int4*)take(sizeof(int4) * n);
+    d->s_key = (int4*)take(sizeof(int4) * n);
+    d->s_pts = (float4*)take(sizeof(float4) * n);
     d->hkey[0] = (uint32_t*)take(sizeof(uint32_t) * n);
     d->hkey[1] = (uint32_t*)take(sizeof(uint32_t) * n);
     d->hval[0] = (uint32_t*)take(sizeof(uint32_t) * n);
@@ -1326,7 +1445,12 @@ void launch_ds_prepare(const DevTree& t, const float* in, int stride, long long 
                        cudaStream_t s) {
     if (n <= 0) return;
     ds_prepare_kernel<<<blocks_for(n, 256), 256, 0, s>>>(t, in, stride, n, ds, d);
-    radix_sort_pairs(d.hkey[0], d.hval[0], d.hkey[1], d.hval[1], n, 1, n, 32, d.temp, s);
+    // 24-bit keys: three passes; the sorted pairs stay where the last pass
+    // left them
+    if (radix_sort_pairs(d.hkey[0], d.hval[0], d.hkey[1], d.hval[1], n, 1, n, DS_HASH_BITS, d.temp, s, false)) {
+        std::swap(d.hkey[0], d.hkey[1]);
+        std::swap(d.hval[0], d.hval[1]);
+    }
     ds_leaders_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, d, t.st);
 }
 

@@ -87,6 +87,8 @@ struct DsScratch {
     float4* box_hi;     // [n]
     float4* mid;        // [n]
     int4* key;          // [n] {kx, ky, kz, clean}
+    int4* s_key;        // [n] key in sorted (hash) order
+    float4* s_pts;      // [n] {x, y, z, input index} in sorted order
     uint32_t* hkey[2];  // [n]
     uint32_t* hval[2];  // [n]
     int* groups;        // [n] leader positions in sorted order
