@@ -30,6 +30,18 @@ __device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4&
                  : "l"(p));
 }
 
+// Slot pairs (256-bit loads) the kNN leaf scan issues together, by the size
+// of the register list.  Measured on the 1M-point uniform map (100k and 1M
+// queries): with k <= 4 in registers and with the shared-memory lists, four
+// pairs at once beat one (k = 1: -8 %, k = 16: -5 %); with 5..8 in registers
+// one pair at a time is faster (k = 5, 1M queries: +10 % with four) — there
+// the candidate insertions, not the loads, set the pace.  Eight pairs lost
+// everywhere (+20..47 %).
+template <int KMAX>
+__host__ __device__ constexpr int knn_leaf_pairs() {
+    return KMAX >= 5 ? 1 : 4;
+}
+
 // Leaves a warp scans per step of the range search's leaf phase.
 #ifndef IKDG_RANGE_LEAF_BATCH
 #define IKDG_RANGE_LEAF_BATCH 4
@@ -230,17 +242,27 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
         const float4* lp = P + (long long)L * LEAF_CAP;
         if (G == 1) {
-            // Two slots per 256-bit load (slot pairs are 32-byte aligned; a
-            // bucket always has LEAF_CAP slots, so the pair never leaves it).
-            for (int j0 = 0; j0 < n; j0 += 2) {
-                float4 a, b;
-                ld_slot_pair(lp + j0, a, b);
-                const uint32_t wa = __float_as_uint(a.w);
-                if (!(wa & F_DEL))
-                    offer(sq_dist(qx, qy, qz, a.x, a.y, a.z), (int)(wa & ID_MASK), L * LEAF_CAP + j0);
-                const uint32_t wb = __float_as_uint(b.w);
-                if (j0 + 1 < n && !(wb & F_DEL))
-                    offer(sq_dist(qx, qy, qz, b.x, b.y, b.z), (int)(wb & ID_MASK), L * LEAF_CAP + j0 + 1);
+            // Two slots per 256-bit load (slot pairs are 32-byte aligned), and
+            // knn_leaf_pairs<KMAX>() loads issued together before any is used.
+            // A bucket always has LEAF_CAP slots in the pool, so loads past
+            // the fill count stay inside it; their slots are ignored.
+            constexpr int PAIRS = knn_leaf_pairs<KMAX>();
+            static_assert(LEAF_CAP % (2 * PAIRS) == 0, "a batch of pairs must not leave the bucket");
+            for (int j0 = 0; j0 < n; j0 += 2 * PAIRS) {
+                float4 pa[PAIRS], pb[PAIRS];
+#pragma unroll
+                for (int u = 0; u < PAIRS; ++u) ld_slot_pair(lp + j0 + 2 * u, pa[u], pb[u]);
+#pragma unroll
+                for (int u = 0; u < PAIRS; ++u) {
+                    const int j = j0 + 2 * u;
+                    const uint32_t wa = __float_as_uint(pa[u].w);
+                    if (j < n && !(wa & F_DEL))
+                        offer(sq_dist(qx, qy, qz, pa[u].x, pa[u].y, pa[u].z), (int)(wa & ID_MASK), L * LEAF_CAP + j);
+                    const uint32_t wb = __float_as_uint(pb[u].w);
+                    if (j + 1 < n && !(wb & F_DEL))
+                        offer(sq_dist(qx, qy, qz, pb[u].x, pb[u].y, pb[u].z), (int)(wb & ID_MASK),
+                              L * LEAF_CAP + j + 1);
+                }
             }
         } else {
           for (int j0 = 0; j0 < n; j0 += G) {
