@@ -869,6 +869,10 @@ __global__ void snapshot_root_kernel(DevTree t) {
 // Bits of the voxel hash the grouper sorts by (and compares: entries of one
 // hash run are the sorted neighbours with equal masked hash).
 constexpr int DS_HASH_BITS = 24;
+// Hash runs longer than this go to ds_fold_big_kernel (a warp per group,
+// DS_BIG_BLOCKS blocks of four warps walking the deferred list).
+constexpr int DS_BIG_RUN = 64;
+constexpr int DS_BIG_BLOCKS = 38;
 
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     h ^= h >> 16;
@@ -1102,6 +1106,7 @@ __device__ __forceinline__ Box3 shfl_box(const Box3& b, int src) {
 __global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, long long a, DsScratch d, float ds) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
+    if (g == 0) *d.n_big = 0;  // ds_fold_kernel lists its deferred groups afresh
     bool active = g < t.st->n_groups && !(t.st->err & ERR_INPUT);  // a non-finite input: the call changes nothing
     long long first = -1;
     int lead = 0;
@@ -1183,8 +1188,13 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
     int j = d.groups[g];
     int4 info = d.g_info[g];
     d.g_out[g] = make_int4(0, 0, 0, 0);
-    if (info.y == -1 && info.x == 0 && group_first_from(d, n, j, a) < 0) return;
     const uint32_t h = __ldg(d.hkey[0] + j);
+    if (j + DS_BIG_RUN < n && __ldg(d.hkey[0] + j + DS_BIG_RUN) == h) {
+        // a long hash run (a voxel with many points): folded by a warp
+        d.big[atomicAdd(d.n_big, 1)] = g;
+        return;
+    }
+    if (info.y == -1 && info.x == 0 && group_first_from(d, n, j, a) < 0) return;
     const int lead = d.hval[0][j];
     const int4 k = __ldg(d.s_key + j);
     float4 mid = d.mid[lead];
@@ -1192,9 +1202,7 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
     const int n0 = info.x;
     bool s_is_s0 = true, del_s0 = false, have_ins = false;
     float cx = 0.f, cy = 0.f, cz = 0.f, cd = 0.f;
-    long long ins_idx = -1;
-    int ins_old_id = -1;  // the winner is an existing point: it keeps its id
-    int cw_old = -1;
+    long long cid = -1;  // id of the current winner c: a stored point keeps its id
     int triggers = 0;
     for_run(d, n, j, h, [&](long long, const int4& kk, const float4& p) {
         if (!same_key(kk, k)) return true;
@@ -1203,12 +1211,12 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
         if (idx >= e) return false;  // members come in increasing index order
         float pd = sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z);
         float wx = p.x, wy = p.y, wz = p.z, wd = pd;
-        int w_old = -1;
+        long long wid = first_id + idx;
         bool trig;
         if (s_is_s0) {
             if (n0 > 0 && best.w < pd) {
                 wx = best.x; wy = best.y; wz = best.z; wd = best.w;
-                w_old = info.z;
+                wid = info.z;
             }
             trig = n0 > 1 || same_point(p.x, p.y, p.z, wx, wy, wz);
             if (trig) {
@@ -1218,30 +1226,144 @@ __global__ void __launch_bounds__(128) ds_fold_kernel(DevTree t, long long n, lo
         } else {
             if (cd < pd) {
                 wx = cx; wy = cy; wz = cz; wd = cd;
-                w_old = cw_old;
+                wid = cid;
             }
             trig = same_point(p.x, p.y, p.z, wx, wy, wz);
         }
         if (trig) {
             ++triggers;
             cx = wx; cy = wy; cz = wz; cd = wd;
-            cw_old = w_old;
+            cid = wid;
             have_ins = true;
-            ins_idx = idx;
-            ins_old_id = w_old;
         }
         return true;
     });
     d.g_out[g] = make_int4(del_s0 ? 1 : 0, have_ins ? 1 : 0, triggers, 0);
     if (triggers) atomicAdd((unsigned long long*)&t.st->count2, (unsigned long long)triggers);
     if (have_ins) {
-        long long id = ins_old_id >= 0 ? (long long)ins_old_id : first_id + ins_idx;
-        if (id > MAX_ID) {
+        if (cid > MAX_ID) {
             atomicOr(&t.st->err, ERR_ID);
             return;
         }
         int q = atomicAdd(&t.st->n_ins, 1);
-        d.ins[q] = make_float4(cx, cy, cz, __int_as_float((int)id));
+        d.ins[q] = make_float4(cx, cy, cz, __int_as_float((int)cid));
+    }
+}
+
+// The fold of ds_fold_kernel for the groups it deferred, one warp per group,
+// 32 members per step.  After the first member the fold's state is the
+// current winner c, and a member p replaces c exactly when d(p) <= d(c) (a
+// later point wins ties): c after member i is the minimum of the members so
+// far and the initial c (the best stored point of the voxel when it has one)
+// under (distance ascending, position descending), a warp prefix minimum.
+// Member i triggers (the voxel's points are replaced) when it replaces c,
+// when it coincides with c (same_point), or, for a voxel holding more than
+// one stored point, when it is the first member.  The point inserted is the
+// final c under its own id (the stored point's, or first_id + its index).
+__global__ void __launch_bounds__(128) ds_fold_big_kernel(DevTree t, long long n, long long a, long long first_id,
+                                                          DsScratch d) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    if (t.st->err & ERR_INPUT) return;
+    const long long e = min(max((long long)t.st->count, a + 1), n);
+    const int nb = *d.n_big;
+    for (int b = warp; b < nb; b += nwarps) {
+        const int g = d.big[b];
+        const int j = d.groups[g];
+        const int4 info = d.g_info[g];
+        const float4 best = d.g_best[g];
+        const uint32_t h = __ldg(d.hkey[0] + j);
+        const int4 k = __ldg(d.s_key + j);
+        const float4 mid = d.mid[d.hval[0][j]];
+        const int n0 = info.x;
+        // running c: distance, position in the run (-2: the stored best,
+        // -1: none), coordinates
+        float cdist = n0 > 0 ? best.w : __int_as_float(0x7f800000);
+        long long cpos = n0 > 0 ? -2 : -1;
+        float cx = best.x, cy = best.y, cz = best.z;
+        long long cid = n0 > 0 ? (long long)info.z : -1;
+        bool first_open = n0 > 1;  // the first member triggers regardless
+        int triggers = 0;
+        bool more = true;
+        for (long long base = j; more && base < n; base += 32) {
+            const long long jj = base + lane;
+            const uint32_t hh = jj < n ? __ldg(d.hkey[0] + jj) : ~h;
+            const unsigned off_run = __ballot_sync(0xffffffffu, hh != h);
+            // entries from the first one of another hash on are not in the run
+            const int run_end = off_run ? __ffs(off_run) - 1 : 32;
+            bool member = false;
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+            long long idx = -1;
+            if (lane < run_end) {
+                const int4 kk = __ldg(d.s_key + jj);
+                if (same_key(kk, k)) {
+                    p = __ldg(d.s_pts + jj);
+                    idx = __float_as_int(p.w);
+                    member = idx >= a && idx < e;
+                }
+            }
+            // members come in increasing index order: one at or past e ends the group
+            const unsigned past = __ballot_sync(0xffffffffu, idx >= e);
+            const int lim = past ? __ffs(past) - 1 : run_end;
+            member = member && lane < lim;
+            if (off_run || past) more = false;
+            const float pd = member ? sq_dist(p.x, p.y, p.z, mid.x, mid.y, mid.z) : __int_as_float(0x7f800000);
+            // inclusive prefix minimum over this step's members
+            float md = pd;
+            int mlane = member ? lane : -1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float od = __shfl_up_sync(0xffffffffu, md, o);
+                const int ol = __shfl_up_sync(0xffffffffu, mlane, o);
+                // (od, ol) is earlier: it stays the minimum only if strictly smaller
+                if (lane >= o && ol >= 0 && (mlane < 0 || od < md)) {
+                    md = od;
+                    mlane = ol;
+                }
+            }
+            // exclusive prefix: the inclusive one of the lane before, then the carry
+            float ed = __shfl_up_sync(0xffffffffu, md, 1);
+            int el = __shfl_up_sync(0xffffffffu, mlane, 1);
+            if (lane == 0) el = -1;
+            // c before this member: the carry unless a member of this step beat it
+            const bool from_step = el >= 0 && ed <= cdist;
+            const float prev_d = from_step ? ed : cdist;
+            const int src = from_step ? el : lane;
+            const float sx = __shfl_sync(0xffffffffu, p.x, src), sy = __shfl_sync(0xffffffffu, p.y, src),
+                        sz = __shfl_sync(0xffffffffu, p.z, src);
+            const float prev_x = from_step ? sx : cx, prev_y = from_step ? sy : cy, prev_z = from_step ? sz : cz;
+            const bool prev_none = !from_step && cpos == -1;
+            const unsigned mem = __ballot_sync(0xffffffffu, member);
+            const bool is_first = first_open && mem != 0 && lane == __ffs(mem) - 1;
+            const bool replaces = member && pd <= prev_d;
+            const bool trig = member && (replaces || is_first ||
+                                         (!prev_none && same_point(p.x, p.y, p.z, prev_x, prev_y, prev_z)));
+            triggers += __popc(__ballot_sync(0xffffffffu, trig));
+            if (mem) first_open = false;
+            // carry: the step's minimum over everything, if it beats c
+            const float sd = __shfl_sync(0xffffffffu, md, 31);
+            const int sl = __shfl_sync(0xffffffffu, mlane, 31);
+            if (sl >= 0 && sd <= cdist) {
+                cdist = sd;
+                cpos = base + sl;
+                cx = __shfl_sync(0xffffffffu, p.x, sl);
+                cy = __shfl_sync(0xffffffffu, p.y, sl);
+                cz = __shfl_sync(0xffffffffu, p.z, sl);
+                cid = first_id + __shfl_sync(0xffffffffu, idx, sl);
+            }
+        }
+        if (lane != 0) continue;
+        const bool have_ins = triggers > 0;
+        d.g_out[g] = make_int4(have_ins && n0 > 0 ? 1 : 0, have_ins ? 1 : 0, triggers, 0);
+        if (!have_ins) continue;
+        atomicAdd((unsigned long long*)&t.st->count2, (unsigned long long)triggers);
+        if (cid > MAX_ID) {
+            atomicOr(&t.st->err, ERR_ID);
+            continue;
+        }
+        const int q = atomicAdd(&t.st->n_ins, 1);
+        d.ins[q] = make_float4(cx, cy, cz, __int_as_float((int)cid));
     }
 }
 
@@ -1411,6 +1533,7 @@ size_t ds_scratch_bytes(long long n) {
     b += au(sizeof(int) * n);          // groups
     b += 2 * au(sizeof(int4) * n);     // g_info, g_out
     b += au(sizeof(float4) * n);       // g_best
+    b += au(sizeof(int) * n) + au(sizeof(int));  // big, n_big
     b += au(sort_temp_bytes(n, 1));
     return b;
 }
@@ -1438,6 +1561,8 @@ void carve_ds_scratch(void* base, long long n, DsScratch* d) {
     d->g_info = (int4*)take(sizeof(int4) * n);
     d->g_out = (int4*)take(sizeof(int4) * n);
     d->g_best = (float4*)take(sizeof(float4) * n);
+    d->big = (int*)take(sizeof(int) * n);
+    d->n_big = (int*)take(sizeof(int));
     d->temp = (void*)p;
 }
 
@@ -1464,6 +1589,7 @@ void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long lo
                     DsScratch& d, int max_groups, cudaStream_t s) {
     if (max_groups <= 0) return;
     ds_fold_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, first_id, d);
+    ds_fold_big_kernel<<<DS_BIG_BLOCKS, 128, 0, s>>>(t, n, a, first_id, d);
     ds_delete_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, aux, d);
 }
 

@@ -96,6 +96,8 @@ struct DsScratch {
     float4* g_best;     // [n] best S0 point {x, y, z, d}
     int4* g_out;        // [n] {delete S0, insert, triggers, -}
     float4* ins;        // [n] points to insert {x, y, z, id}
+    int* big;           // [n] groups deferred to the warp fold
+    int* n_big;         // [1]
     void* temp;
 };
 size_t ds_scratch_bytes(long long n);

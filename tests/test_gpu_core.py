@@ -224,6 +224,41 @@ def test_downsample_voxel_boundaries(ikdg_mod):
     assert_same_valid(tree, ref)
 
 
+def test_downsample_dense_voxels(ikdg_mod):
+    # Hundreds of new points in one voxel (the long hash runs folded by a warp)
+    # with 0, 1 and 3 stored points, a stored point at the exact centre that
+    # only coincident points can displace, distance ties between new points
+    # (the later one wins) and exact duplicates, interleaved in input order.
+    ds = np.float32(0.5)
+    rng = np.random.default_rng(41)
+
+    def in_voxel(cell, m):
+        lo = np.asarray(cell, np.float32) * ds
+        return (lo + rng.uniform(0.01, 0.49, (m, 3))).astype(np.float32)
+
+    centre4 = (np.asarray([-30, 8, 2], np.float32) * ds + ds / 2).astype(np.float32)
+    base = np.concatenate([rng.uniform(-5, 5, (3000, 3)).astype(np.float32),
+                           in_voxel((30, 30, 30), 1), in_voxel((-30, 30, 30), 3), centre4[None]])
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, float(ds)), spec.SpecTree(float(ds))
+    tree.Build(base)
+    ref.Build(base)
+    for it in range(2):
+        # one ulp off the stored centre point: farther from the centre but the
+        # same point (|a - b| < 1e-6), so the stored point stays the winner
+        nudged = np.nextafter(centre4, np.float32(np.inf))[None].repeat(30, 0)
+        parts = [in_voxel((40, 40, 40), 900), in_voxel((30, 30, 30), 700), in_voxel((-30, 30, 30), 600),
+                 np.repeat(centre4[None], 40, 0), nudged, in_voxel((-30, 8, 2), 300)]
+        # mirrored pairs about the centre of voxel (40, 40, 40): equal distances
+        c1 = (np.asarray([40, 40, 40], np.float32) * ds + ds / 2).astype(np.float32)
+        off = rng.uniform(0.01, 0.2, (100, 3)).astype(np.float32)
+        parts += [c1 + off, c1 - off]
+        add = np.concatenate(parts)
+        add = np.concatenate([add, add[rng.choice(len(add), 200)]])  # exact duplicates
+        add = add[rng.permutation(len(add))]
+        assert tree.Add_Points(add, True) == ref.Add_Points(add, True)
+        assert_same_valid(tree, ref)
+
+
 def test_growth_and_rebalance(ikdg_mod):
     # All inserts land in one corner: leaf overflow splits, scapegoat rebuilds,
     # pool growth.
