@@ -20,7 +20,7 @@ constexpr int KNN_THREADS = IKDG_KNN_THREADS;
 
 // STAGED: the outputs are host memory (rows leave through shared memory as
 // coalesced 16-byte stores; see knn_body).
-template <int KMAX, int G, bool STAGED = false>
+template <int KMAX, int G, bool STAGED = false, int PAIRS = search::knn_leaf_pairs<KMAX>()>
 __global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float* __restrict__ q, int q_stride,
                                                   long long nq, int k, float max_sq, int* __restrict__ out_id,
                                                   float* __restrict__ out_d2, float* __restrict__ out_xyz,
@@ -30,11 +30,12 @@ __global__ void __launch_bounds__(KNN_THREADS) knn_kernel(DevTree t, const float
     if constexpr (KMAX > 0 && G == 1 && STAGED) {
         // rows of a warp's consecutive queries leave through shared memory
         __shared__ __align__(16) float stage[KNN_THREADS / 32][search::knn_stage_floats(KMAX)];
-        search::knn_body<KMAX, G>(t, gtid, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots, perm,
-                                  nullptr, nullptr, nullptr, 1, perm == nullptr ? stage[threadIdx.x >> 5] : nullptr);
+        search::knn_body<KMAX, G, PAIRS>(t, gtid, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots,
+                                         perm, nullptr, nullptr, nullptr, 1,
+                                         perm == nullptr ? stage[threadIdx.x >> 5] : nullptr);
     } else {
-        search::knn_body<KMAX, G>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt, slots,
-                                  perm);
+        search::knn_body<KMAX, G, PAIRS>(t, gtid / G, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, out_cnt,
+                                         slots, perm);
     }
 }
 
@@ -71,6 +72,17 @@ __global__ void __launch_bounds__(128) range_kernel(DevTree t, const float* __re
 
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// Blocks of `fn` resident on the whole GPU (0 if the query fails).
+inline int knn_resident(const void* fn) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, KNN_THREADS, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms * per_sm;
+}
+
 template <int KMAX>
 void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, int k, float max_sq, int* out_id,
                 float* out_d2, float* out_xyz, int* out_cnt, int* slots, const int* perm, int lanes, cudaStream_t s,
@@ -78,9 +90,29 @@ void knn_launch(const DevTree& t, const float* q, int q_stride, long long nq, in
     const int G = lanes >= 4 ? 4 : lanes == 2 ? 2 : 1;
     const unsigned grid = blocks_for(nq * G, KNN_THREADS);
     if constexpr (KMAX > 0) {
-        if (host_out && G == 1 && perm == nullptr) {
-            knn_kernel<KMAX, 1, true><<<grid, KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2,
-                                                                   out_xyz, out_cnt, slots, perm);
+        if (G == 1) {
+            // Four slot pairs per leaf step while every block of the batch is
+            // resident at once (the occupancy of a kernel does not change:
+            // looked up once; the library drives one kind of GPU).
+            const bool staged = host_out && perm == nullptr;
+            static int resident[2] = {-1, -1};
+            int& r = resident[staged ? 1 : 0];
+            if (r < 0)
+                r = staged ? knn_resident((const void*)knn_kernel<KMAX, 1, true, 4>)
+                           : knn_resident((const void*)knn_kernel<KMAX, 1, false, 4>);
+            const bool wide = grid <= (unsigned)r;
+#define IKDG_KNN_P(ST, P)                                                                                     \
+    knn_kernel<KMAX, 1, ST, P><<<grid, KNN_THREADS, 0, s>>>(t, q, q_stride, nq, k, max_sq, out_id, out_d2, out_xyz, \
+                                                            out_cnt, slots, perm)
+            if (staged && wide)
+                IKDG_KNN_P(true, 4);
+            else if (staged)
+                IKDG_KNN_P(true, 2);
+            else if (wide)
+                IKDG_KNN_P(false, 4);
+            else
+                IKDG_KNN_P(false, 2);
+#undef IKDG_KNN_P
             return;
         }
     }

@@ -30,16 +30,15 @@ __device__ __forceinline__ void ld_slot_pair(const float4* p, float4& a, float4&
                  : "l"(p));
 }
 
-// Slot pairs (256-bit loads) the kNN leaf scan issues together, by the size
-// of the register list.  Measured on the 1M-point uniform map (100k and 1M
-// queries): with k <= 4 in registers and with the shared-memory lists, four
-// pairs at once beat one (k = 1: -8 %, k = 16: -5 %); with 5..8 in registers
-// one pair at a time is faster (k = 5, 1M queries: +10 % with four) — there
-// the candidate insertions, not the loads, set the pace.  Eight pairs lost
-// everywhere (+20..47 %).
+// Slot pairs (256-bit loads) the kNN leaf scan issues together: the default
+// for the register lists is two; the per-call kNN picks four when the whole
+// batch is resident at once (measured, 1M-point map, k = 5: 100k queries
+// 0.155 -> 0.146 ms with four; 1M queries 0.851 -> 0.825 ms with two, 0.896
+// with four, whose extra registers cost resident blocks).  The shared-memory
+// and row lists take four.
 template <int KMAX>
 __host__ __device__ constexpr int knn_leaf_pairs() {
-    return KMAX >= 5 ? 1 : 4;
+    return KMAX > 0 ? 2 : 4;
 }
 
 // Leaves a warp scans per step of the range search's leaf phase.
@@ -87,7 +86,7 @@ __device__ __forceinline__ bool cand_less(float d, int id, float d2, int id2) {
 // in lane order, which keeps the copies identical.
 // `tid` is the query (before the optional permutation `perm`) of this
 // thread's group; every lane of the warp must call this together.
-template <int KMAX, int G>
+template <int KMAX, int G, int PAIRS = knn_leaf_pairs<KMAX>()>
 __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const float* __restrict__ q, int q_stride,
                                          long long nq, int k, float max_sq, int* __restrict__ out_id,
                                          float* __restrict__ out_d2, float* __restrict__ out_xyz,
@@ -242,12 +241,20 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
         const int n = min(__ldg(t.leaf_n + L), LEAF_CAP);
         const float4* lp = P + (long long)L * LEAF_CAP;
         if (G == 1) {
+            // Two passes.  First every slot's distance is checked against the
+            // current bound, marking the slots that can enter the list (no
+            // branch: lanes stay converged); then only the marked slots are
+            // offered, re-read from L1.  Offering in one pass made the warp run
+            // the insertion for every slot at which any lane had a candidate.
+            // The final list does not depend on the order of the offers, and
+            // the bound only tightens, so the marks miss nothing.
             // Two slots per 256-bit load (slot pairs are 32-byte aligned), and
-            // knn_leaf_pairs<KMAX>() loads issued together before any is used.
+            // PAIRS loads issued together before any is used.
             // A bucket always has LEAF_CAP slots in the pool, so loads past
             // the fill count stay inside it; their slots are ignored.
-            constexpr int PAIRS = knn_leaf_pairs<KMAX>();
             static_assert(LEAF_CAP % (2 * PAIRS) == 0, "a batch of pairs must not leave the bucket");
+            static_assert(LEAF_CAP <= 32, "one mark bit per slot");
+            uint32_t marks = 0;
             for (int j0 = 0; j0 < n; j0 += 2 * PAIRS) {
                 float4 pa[PAIRS], pb[PAIRS];
 #pragma unroll
@@ -256,13 +263,23 @@ __device__ __forceinline__ void knn_body(const DevTree& t, long long tid, const 
                 for (int u = 0; u < PAIRS; ++u) {
                     const int j = j0 + 2 * u;
                     const uint32_t wa = __float_as_uint(pa[u].w);
-                    if (j < n && !(wa & F_DEL))
-                        offer(sq_dist(qx, qy, qz, pa[u].x, pa[u].y, pa[u].z), (int)(wa & ID_MASK), L * LEAF_CAP + j);
+                    const float da = sq_dist(qx, qy, qz, pa[u].x, pa[u].y, pa[u].z);
+                    const bool ma = j < n && !(wa & F_DEL) && da <= max_sq &&
+                                    cand_less(da, (int)(wa & ID_MASK), worst, worst_id);
                     const uint32_t wb = __float_as_uint(pb[u].w);
-                    if (j + 1 < n && !(wb & F_DEL))
-                        offer(sq_dist(qx, qy, qz, pb[u].x, pb[u].y, pb[u].z), (int)(wb & ID_MASK),
-                              L * LEAF_CAP + j + 1);
+                    const float db = sq_dist(qx, qy, qz, pb[u].x, pb[u].y, pb[u].z);
+                    const bool mb = j + 1 < n && !(wb & F_DEL) && db <= max_sq &&
+                                    cand_less(db, (int)(wb & ID_MASK), worst, worst_id);
+                    marks |= (ma ? 1u : 0u) << j;
+                    marks |= (mb ? 1u : 0u) << (j + 1);
                 }
+            }
+            while (marks) {
+                const int j = __ffs(marks) - 1;
+                marks &= marks - 1;
+                const float4 p = __ldg(lp + j);
+                const uint32_t w = __float_as_uint(p.w);
+                offer(sq_dist(qx, qy, qz, p.x, p.y, p.z), (int)(w & ID_MASK), L * LEAF_CAP + j);
             }
         } else {
           for (int j0 = 0; j0 < n; j0 += G) {
