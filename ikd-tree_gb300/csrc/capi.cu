@@ -404,10 +404,14 @@ struct Tree {
     // refit their ancestors.
     // bound: an upper bound on the jobs selected (the violator count); the
     // job counts, totals and sizes come back in one status read.
-    void run_jobs(int bound, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound) {
-        small.ensure(scan_temp_bytes(bound + 1) + 1024, stream);
-        launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, bound, small.p, stream);
-        read_status();
+    // counted: the jobs were selected and counted before the last status read
+    // (launch_select_and_count), which brought their count and sizes back.
+    void run_jobs(int bound, const int4* ovf_leaf, const float4* ovf_pts, int ovf_bound, bool counted = false) {
+        if (!counted) {
+            small.ensure(scan_temp_bytes(bound + 1) + 1024, stream);
+            launch_job_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, bound, small.p, stream);
+            read_status();
+        }
         const int nj = st->n_jobs;
         if (nj == 0) throw Internal{"violators without a topmost job"};
         if (debug_validate) {
@@ -483,6 +487,15 @@ struct Tree {
         bool settled = false;
         for (int round = 0; round < 8; ++round) {
             launch_snapshot_root(dt, stream);
+            // The first round selects and counts its rebuild jobs before the
+            // status read (nothing happens on the device when there are no
+            // violators), so one read brings the violators, the jobs and
+            // their sizes.  After a mutation no build ran since the last
+            // read, so the host's pool tops bound the leaf and node scans;
+            // later rounds, and the call after rebuild_all's build, read
+            // first.
+            const bool ahead = round == 0 && refit_first;
+            if (ahead) launch_select_and_count(dt, aux, st->leaf_top, st->node_top, ovf_leaf, ovf_bound, stream);
             read_status();
             int nv = st->n_viol;
             if (nv == 0) {
@@ -494,10 +507,11 @@ struct Tree {
                 launch_clear_viol(dt, aux, nv, stream);
                 break;
             }
-            launch_select_jobs(dt, aux, nv, stream);
+            if (!ahead) launch_select_jobs(dt, aux, nv, stream);
             dbg_round = round;
             // at most nv jobs: run_jobs reads the job count with its own sizes
-            run_jobs(nv, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0);
+            run_jobs(nv, round == 0 ? ovf_leaf : nullptr, round == 0 ? ovf_pts : nullptr, round == 0 ? ovf_bound : 0,
+                     ahead);
             zero_fields(offsetof(DevStatus, n_items), sizeof(int));
             if (debug_validate) {
                 read_status();

@@ -143,12 +143,21 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         Box3 b = empty_box();
         int del = 0;
         const float4* lpn = t.pts + (long long)L * LEAF_CAP;
-        for (int j = 0; j < m; ++j) {
-            float4 p = __ldcg(lpn + j);
-            if (__float_as_uint(p.w) & F_DEL)
-                ++del;
-            else
-                box_grow(b, p.x, p.y, p.z);
+        // eight slot loads in flight (a bucket always has LEAF_CAP slots, so
+        // the loads past the fill count stay inside it and are ignored)
+        static_assert(LEAF_CAP % 8 == 0, "slot batches must not leave the bucket");
+        for (int j0 = 0; j0 < m; j0 += 8) {
+            float4 pb[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) pb[u] = __ldcg(lpn + j0 + u);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (j0 + u >= m) break;
+                if (__float_as_uint(pb[u].w) & F_DEL)
+                    ++del;
+                else
+                    box_grow(b, pb[u].x, pb[u].y, pb[u].z);
+            }
         }
         write_child_box(t.node, X, llp & 1, b);
         write_child_cnt(t.ncnt, X, llp & 1, n, del);
@@ -163,10 +172,13 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
             atomicOr(&t.st->err, ERR_LOOP);
             return;
         }
-        __threadfence();  // release: this walker's writes into X's record
-        int old = atomicAdd(&a.arrive[X], 1);
+        // One acq_rel atomic: it releases this walker's writes into X's record
+        // and, for the last walker, acquires the other children's (the
+        // fence.sc / atomic / fence.sc form it replaces cost ~20 us per LiDAR
+        // scan).
+        int old;
+        asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(&a.arrive[X]) : "memory");
         if (old + 1 < expect) return;
-        __threadfence();  // acquire: the other children's writes are visible
         a.pend[X] = 0;
         a.arrive[X] = 0;
         const int P = lp >> 1;
@@ -220,9 +232,7 @@ __global__ void clear_dirty_kernel(UpdateAux a, const int* n_items) {
 
 // ---- rebuild jobs ----------------------------------------------------------------
 
-__global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_viol || i >= a.list_cap) return;
+__device__ __forceinline__ void select_job(const DevTree& t, const UpdateAux& a, int i) {
     int code = a.viol[i];
     int link = code < 0 ? t.lparent[code_leaf(code)] : t.nparent[code];
     if (link < 0) return;
@@ -251,12 +261,22 @@ __global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
         a.job_of_node[code] = j;
 }
 
-__global__ void clear_viol_kernel(UpdateAux a, const int* n_viol) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_viol || i >= a.list_cap) return;
-    int code = a.viol[i];
-    if (code > 0) a.viol_flag[code] = 0;
+// Grid-stride over the violators: the grid may be sized by a host bound or,
+// when the selection runs before the host has read the violator count, by a
+// fixed number of blocks.
+__global__ void select_jobs_kernel(DevTree t, UpdateAux a, const int* n_viol) {
+    const int nv = min(*n_viol, a.list_cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) select_job(t, a, i);
 }
+
+__global__ void clear_viol_kernel(UpdateAux a, const int* n_viol) {
+    const int nv = min(*n_viol, a.list_cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+        int code = a.viol[i];
+        if (code > 0) a.viol_flag[code] = 0;
+    }
+}
+
 
 __device__ __forceinline__ int find_job_up(const DevTree& t, const UpdateAux& a, int X) {
     for (int steps = 0; X > 0; ++steps) {
@@ -275,14 +295,21 @@ __device__ __forceinline__ int count_valid(const DevTree& t, int L) {
     int n = t.leaf_n[L];
     int m = n < LEAF_CAP ? n : LEAF_CAP;
     int v = 0;
-    const float4* lp = t.pts + (long long)L * LEAF_CAP;
-    for (int j = 0; j < m; ++j) v += (__float_as_uint(lp[j].w) & F_DEL) ? 0 : 1;
+    const float* lw = reinterpret_cast<const float*>(t.pts + (long long)L * LEAF_CAP) + 3;
+    // eight flag words in flight (slots past the fill count stay in the bucket)
+    for (int j0 = 0; j0 < m; j0 += 8) {
+        float w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = lw[4 * (j0 + u)];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v += (j0 + u < m && !(__float_as_uint(w[u]) & F_DEL)) ? 1 : 0;
+    }
     return v;
 }
 
 __global__ void job_count_leaf_kernel(DevTree t, UpdateAux a, int leaf_top) {
     int L = blockIdx.x * blockDim.x + threadIdx.x;
-    if (L >= leaf_top) return;
+    if (L >= leaf_top || t.st->n_jobs == 0) return;  // nothing selected: the speculative count ends here
     int lp = t.lparent[L];
     if (lp < 0) {
         a.leaf_job[L] = -1;
@@ -296,7 +323,7 @@ __global__ void job_count_leaf_kernel(DevTree t, UpdateAux a, int leaf_top) {
 
 __global__ void job_count_node_kernel(DevTree t, UpdateAux a, int node_top) {
     int X = blockIdx.x * blockDim.x + threadIdx.x;
-    if (X < 1 || X >= node_top) return;
+    if (X < 1 || X >= node_top || t.st->n_jobs == 0) return;
     if (t.nparent[X] < 0) {
         a.node_job[X] = -1;
         return;
@@ -306,7 +333,7 @@ __global__ void job_count_node_kernel(DevTree t, UpdateAux a, int node_top) {
 
 __global__ void job_count_ovf_kernel(DevTree t, UpdateAux a, const int4* __restrict__ ovf_leaf, const int* n_ovf) {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= *n_ovf) return;
+    if (o >= *n_ovf || t.st->n_jobs == 0) return;
     int L = ovf_leaf[o].x;
     int j = a.leaf_job[L];
     if (j < 0) {
@@ -326,6 +353,55 @@ __global__ void job_count_ovf_kernel(DevTree t, UpdateAux a, const int4* __restr
         return;
     }
     atomicAdd(&a.job_count[j], 1);
+}
+
+// job_off = exclusive prefix sum of job_count over the selected jobs (count
+// read on the device), job_off[n_jobs] = st->job_total = the sum, st->max_job
+// = the largest job: one block, 1,024 jobs per step.
+__global__ void __launch_bounds__(1024) job_scan_kernel(DevTree t, UpdateAux a) {
+    __shared__ int wsum[32];
+    __shared__ int carry, mx;
+    const int n = min(t.st->n_jobs, a.list_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        mx = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < n ? a.job_count[i] : 0;
+        int inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[w] = inc;
+        if (v > 0) atomicMax(&mx, v);
+        __syncthreads();
+        if (w == 0) {
+            const int ws = wsum[lane];
+            int wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            wsum[lane] = wi - ws;
+        }
+        __syncthreads();
+        const int c = carry;
+        if (i < n) a.job_off[i] = c + wsum[w] + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + wsum[w] + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        a.job_off[n] = carry;
+        t.st->job_total = carry;
+        t.st->max_job = mx;
+    }
 }
 
 __global__ void job_max_kernel(DevTree t, UpdateAux a, const int* n_jobs, const int* total) {
@@ -349,16 +425,23 @@ __global__ void job_gather_leaf_kernel(DevTree t, UpdateAux a, int leaf_top, flo
     const float4* lp = t.pts + (long long)L * LEAF_CAP;
     int nv = count_valid(t, L);
     int pos = a.job_off[j] + atomicAdd(&a.job_fill[j], nv);
-    for (int s = 0; s < m; ++s) {
-        float4 p = lp[s];
-        uint32_t w = __float_as_uint(p.w);
-        if (!(w & F_DEL)) {
-            out[pos++] = p;
-        } else if (!(w & F_DSDEL)) {
-            // Dropped deleted points are kept for acquire_removed_points
-            // (flatten with DELETE_POINTS_REC, ikd_Tree.cpp:1338-1342).
-            long long r = atomicAdd((unsigned long long*)&t.st->removed_n, 1ull);
-            if (r < removed_cap) removed[r] = make_float4(p.x, p.y, p.z, __uint_as_float(w & ID_MASK));
+    for (int s0 = 0; s0 < m; s0 += 8) {
+        float4 pb[8];  // eight slots in flight (the bucket always has LEAF_CAP slots)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) pb[u] = lp[s0 + u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (s0 + u >= m) break;
+            const float4 p = pb[u];
+            const uint32_t w = __float_as_uint(p.w);
+            if (!(w & F_DEL)) {
+                out[pos++] = p;
+            } else if (!(w & F_DSDEL)) {
+                // Dropped deleted points are kept for acquire_removed_points
+                // (flatten with DELETE_POINTS_REC, ikd_Tree.cpp:1338-1342).
+                long long r = atomicAdd((unsigned long long*)&t.st->removed_n, 1ull);
+                if (r < removed_cap) removed[r] = make_float4(p.x, p.y, p.z, __uint_as_float(w & ID_MASK));
+            }
         }
     }
     t.lparent[L] = -1;
@@ -873,6 +956,8 @@ constexpr int DS_HASH_BITS = 24;
 // DS_BIG_BLOCKS blocks of four warps walking the deferred list).
 constexpr int DS_BIG_RUN = 64;
 constexpr int DS_BIG_BLOCKS = 38;
+// Blocks of the job selection when it runs before the violator count is known.
+constexpr int SPEC_BLOCKS = 152;
 
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {
     h ^= h >> 16;
@@ -1449,6 +1534,17 @@ void launch_job_count(const DevTree& t, const UpdateAux& a, int leaf_top, int no
     // entries are zero); the total lands in job_count[max_jobs].
     exclusive_scan(a.job_count, a.job_off, max_jobs, a.job_off + max_jobs, scan_temp, s);
     job_max_kernel<<<blocks_for(max_jobs, 256), 256, 0, s>>>(t, a, &t.st->n_jobs, a.job_off + max_jobs);
+}
+
+void launch_select_and_count(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
+                             int max_ovf, cudaStream_t s) {
+    // the violator count is only on the device: fixed grids, grid-stride loops
+    select_jobs_kernel<<<SPEC_BLOCKS, 256, 0, s>>>(t, a, &t.st->n_viol);
+    clear_viol_kernel<<<SPEC_BLOCKS, 256, 0, s>>>(a, &t.st->n_viol);
+    if (leaf_top > 0) job_count_leaf_kernel<<<blocks_for(leaf_top, 256), 256, 0, s>>>(t, a, leaf_top);
+    if (node_top > 1) job_count_node_kernel<<<blocks_for(node_top, 256), 256, 0, s>>>(t, a, node_top);
+    if (max_ovf > 0) job_count_ovf_kernel<<<blocks_for(max_ovf, 256), 256, 0, s>>>(t, a, ovf_leaf, &t.st->n_ovf);
+    job_scan_kernel<<<1, 1024, 0, s>>>(t, a);
 }
 
 void launch_job_gather(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,

@@ -46,6 +46,12 @@ void launch_clear_viol(const DevTree& t, const UpdateAux& a, int max_viol, cudaS
 // Count / gather the valid points of every job (plus overflow points).
 void launch_job_count(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
                       int max_ovf, int max_jobs, void* scan_temp, cudaStream_t s);
+// Job selection and counting launched before the host knows the violator
+// count (st->n_viol, st->n_jobs read on the device; nothing happens when they
+// are zero): one status read then returns the violators, the jobs and their
+// sizes.  leaf_top / node_top must be current (no build since the last read).
+void launch_select_and_count(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
+                             int max_ovf, cudaStream_t s);
 void launch_job_gather(const DevTree& t, const UpdateAux& a, int leaf_top, int node_top, const int4* ovf_leaf,
                        const float4* ovf_pts, int max_ovf, float4* out, float4* removed, long long removed_cap,
                        cudaStream_t s);
