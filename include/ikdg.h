@@ -120,10 +120,10 @@ int ikdg_knn_device(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, in
  * until the process exits); smaller batches are searched unsorted and use no
  * scratch.  Limits: nq <= 262144 queries and k <= 64 per call; larger
  * requests fail with IKDG_BAD_ARG.  The first call on a device looks the
- * array up (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's contents:
- * calls that can overlap on the GPU (for example on two trees with different
- * streams) race on it and must be serialised by the caller.  Pointers are
+ * array up (cudaGetSymbolAddress).  All calls share the array and it keeps
+ * the last call's contents: calls that can overlap on the GPU (for example on
+ * two trees with different streams) race on it and must be serialised by the
+ * caller.  Pointers are
  * device pointers; asynchronous on the tree's stream; results equal
  * ikdg_knn_device's. */
 int ikdg_knn_device_noalloc(ikdg_tree* t, const float* q, int64_t nq, int32_t stride, int32_t k, double max_dist,
