@@ -588,7 +588,6 @@ constexpr int MID_MAX = 1 << 17;
 constexpr int MID_THREADS = 1024;
 constexpr int MID_PPT = 4;
 constexpr int MID_TILE = MID_THREADS * MID_PPT;
-constexpr int MID_BATCH = 4;  // loads in flight per thread in the AABB and histogram passes
 
 struct MidShared {
     int hist[256];
@@ -654,24 +653,14 @@ __global__ void __launch_bounds__(MID_THREADS, 1) mid_level_kernel(DevTree t, co
             }
             continue;
         }
-        // AABB.  The passes over the segment issue MID_BATCH loads per thread
-        // before using any (one L2 round trip per batch, not per point).
+        // AABB.
         uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
-        for (int base = s + tid; base < e; base += MID_BATCH * MID_THREADS) {
-            float4 pb[MID_BATCH];
-#pragma unroll
-            for (int u = 0; u < MID_BATCH; ++u) {
-                const int i = base + u * MID_THREADS;
-                if (i < e) pb[u] = src[i];
-            }
-#pragma unroll
-            for (int u = 0; u < MID_BATCH; ++u) {
-                if (base + u * MID_THREADS >= e) break;
-                const uint32_t kx = float_key(pb[u].x), ky = float_key(pb[u].y), kz = float_key(pb[u].z);
-                mn[0] = min(mn[0], kx), mx[0] = max(mx[0], kx);
-                mn[1] = min(mn[1], ky), mx[1] = max(mx[1], ky);
-                mn[2] = min(mn[2], kz), mx[2] = max(mx[2], kz);
-            }
+        for (int i = s + tid; i < e; i += MID_THREADS) {
+            const float4 p = src[i];
+            const uint32_t kx = float_key(p.x), ky = float_key(p.y), kz = float_key(p.z);
+            mn[0] = min(mn[0], kx), mx[0] = max(mx[0], kx);
+            mn[1] = min(mn[1], ky), mx[1] = max(mx[1], ky);
+            mn[2] = min(mn[2], kz), mx[2] = max(mx[2], kz);
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -729,24 +718,22 @@ __global__ void __launch_bounds__(MID_THREADS, 1) mid_level_kernel(DevTree t, co
             const int shift = 24 - 8 * pass;
             if (tid < 256) sm.hist[tid] = 0;
             __syncthreads();
-            for (int base = s; base < e; base += MID_BATCH * MID_THREADS) {
-                uint32_t kb[MID_BATCH];
-#pragma unroll
-                for (int u = 0; u < MID_BATCH; ++u) {
-                    const int i = base + u * MID_THREADS + tid;
-                    kb[u] = 0;
-                    if (i < e) kb[u] = pass == 0 ? float_key(coord4(src[i], axis)) : keys[i];
+            for (int base = s; base < e; base += MID_THREADS) {
+                const int i = base + tid;
+                bool ok = false;
+                uint32_t k = 0;
+                if (i < e) {
+                    if (pass == 0) {
+                        k = float_key(coord4(src[i], axis));
+                        keys[i] = k;
+                    } else {
+                        k = keys[i];
+                    }
+                    ok = (k & pmask) == prefix;
                 }
-#pragma unroll
-                for (int u = 0; u < MID_BATCH; ++u) {
-                    const int i = base + u * MID_THREADS + tid;
-                    const uint32_t k = kb[u];
-                    if (pass == 0 && i < e) keys[i] = k;
-                    const bool ok = i < e && (k & pmask) == prefix;
-                    const int d = ok ? (int)((k >> shift) & 255u) : 256 + lane;
-                    const unsigned peers = __match_any_sync(0xffffffffu, d);
-                    if (ok && lane == __ffs(peers) - 1) atomicAdd(&sm.hist[d], __popc(peers));
-                }
+                const int d = ok ? (int)((k >> shift) & 255u) : 256 + lane;
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                if (ok && lane == __ffs(peers) - 1) atomicAdd(&sm.hist[d], __popc(peers));
             }
             __syncthreads();
             if (warp == 0) {
@@ -790,17 +777,13 @@ __global__ void __launch_bounds__(MID_THREADS, 1) mid_level_kernel(DevTree t, co
         for (int base = s; base < e; base += MID_TILE) {
             const int i0 = base + tid * MID_PPT;
             uint32_t kk[MID_PPT];
-            float4 pp[MID_PPT];
             uint32_t sum = 0;
 #pragma unroll
             for (int r = 0; r < MID_PPT; ++r) {
                 const int i = i0 + r;
                 kk[r] = i < e ? keys[i] : 0xffffffffu;
-                if (i < e) pp[r] = src[i];  // loaded with the keys, stored after the scan
+                if (i < e) sum += kk[r] < v ? 1u : (kk[r] == v ? 0x10000u : 0u);
             }
-#pragma unroll
-            for (int r = 0; r < MID_PPT; ++r)
-                if (i0 + r < e) sum += kk[r] < v ? 1u : (kk[r] == v ? 0x10000u : 0u);
             uint32_t total;
             const uint32_t ex = mid_block_scan(sum, sm.wsum, &sm.tot, &total);
             uint32_t lt = carry_lt + (ex & 0xffffu), eq = carry_eq + (ex >> 16);
@@ -812,7 +795,7 @@ __global__ void __launch_bounds__(MID_THREADS, 1) mid_level_kernel(DevTree t, co
                 const bool left = k < v || (k == v && eq < need);
                 const uint32_t lb = lt + (eq < need ? eq : need);
                 const int dest = left ? s + (int)lb : s + m + (i - s - (int)lb);
-                if (dest >= s && dest < e) dst[dest] = pp[r];
+                if (dest >= s && dest < e) dst[dest] = src[i];
                 else atomicOr(&t.st->err, ERR_SEG);  // cannot happen: the select found rank m
                 if (k < v) ++lt;
                 else if (k == v) ++eq;

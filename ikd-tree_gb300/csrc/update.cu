@@ -143,21 +143,12 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
         Box3 b = empty_box();
         int del = 0;
         const float4* lpn = t.pts + (long long)L * LEAF_CAP;
-        // eight slot loads in flight (a bucket always has LEAF_CAP slots, so
-        // the loads past the fill count stay inside it and are ignored)
-        static_assert(LEAF_CAP % 8 == 0, "slot batches must not leave the bucket");
-        for (int j0 = 0; j0 < m; j0 += 8) {
-            float4 pb[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) pb[u] = __ldcg(lpn + j0 + u);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (j0 + u >= m) break;
-                if (__float_as_uint(pb[u].w) & F_DEL)
-                    ++del;
-                else
-                    box_grow(b, pb[u].x, pb[u].y, pb[u].z);
-            }
+        for (int j = 0; j < m; ++j) {
+            float4 p = __ldcg(lpn + j);
+            if (__float_as_uint(p.w) & F_DEL)
+                ++del;
+            else
+                box_grow(b, p.x, p.y, p.z);
         }
         write_child_box(t.node, X, llp & 1, b);
         write_child_cnt(t.ncnt, X, llp & 1, n, del);
