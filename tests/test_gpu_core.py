@@ -259,6 +259,42 @@ def test_downsample_dense_voxels(ikdg_mod):
         assert_same_valid(tree, ref)
 
 
+def test_downsample_dense_voxel_split_by_slivers(ikdg_mod):
+    # A voxel with hundreds of new points whose run is cut into several
+    # sub-batches by points on voxel faces (one ulp either side), which are
+    # folded alone: the warp fold must stop at each sub-batch end and resume.
+    ds = np.float32(0.2)
+    rng = np.random.default_rng(43)
+    lo = np.asarray([7, -3, 2], np.float32) * ds
+    dense = (lo + rng.uniform(0.005, 0.195, (700, 3))).astype(np.float32)
+    # coordinates near voxel faces whose float voxel box misses them or whose
+    # neighbour's box also holds them (the library folds such points alone)
+    k = np.arange(-200, 200, dtype=np.float32)
+    faces = (k * ds).astype(np.float32)
+    near = np.concatenate([faces, np.nextafter(faces, np.float32(np.inf)), np.nextafter(faces, -np.float32(np.inf))])
+
+    def in_box(c, f):
+        b_lo = np.float32(f * ds)
+        return (b_lo <= c) & (c < np.float32(b_lo + ds))
+
+    f = np.floor(near / ds).astype(np.float32)
+    sliver = ~in_box(near, f) | in_box(near, f - 1) | in_box(near, f + 1)
+    assert sliver.sum() > 20
+    slivers = np.stack([rng.choice(near[sliver], 12), rng.uniform(-1, 1, 12), rng.uniform(-1, 1, 12)], 1)
+    slivers = slivers.astype(np.float32)
+    add = dense.copy()
+    cut = np.sort(rng.choice(np.arange(50, 650), 12, replace=False))
+    add = np.insert(add, cut, slivers, axis=0)
+    base = np.concatenate([rng.uniform(-1, 2, (1500, 3)).astype(np.float32), dense[:2] + np.float32(0.001)])
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, float(ds)), spec.SpecTree(float(ds))
+    tree.Build(base)
+    ref.Build(base)
+    for it in range(2):
+        assert tree.Add_Points(add, True) == ref.Add_Points(add, True)
+        assert_same_valid(tree, ref)
+        add = add[rng.permutation(len(add))]
+
+
 def test_growth_and_rebalance(ikdg_mod):
     # All inserts land in one corner: leaf overflow splits, scapegoat rebuilds,
     # pool growth.
