@@ -263,6 +263,8 @@ struct LbShared {
     int8_t saxis[SEGS];        // split axis, -1 for leaves
     uint32_t wsum[THREADS / 32];
     PoolRun run_leaf, run_node;
+    int free_leaf_n, free_node_n;  // free-stack sizes when the runs were taken
+    uint32_t level_total;          // leaves (low 16 bits) and nodes of the current level
     int nseg[2];
     int overflow;
 };
@@ -297,6 +299,41 @@ __device__ void lb_bitonic3(unsigned long long (*K)[MAXN], int size) {
             __syncthreads();
         }
     }
+}
+
+// Nodes and leaves of the subtree the builders make from n points with leaf
+// fill `fill`: a segment of more than `fill` points is a node whose children
+// hold n / 2 and n - n / 2 points, so the sizes of one level take at most two
+// consecutive values.
+__device__ __forceinline__ void subtree_counts(int n, int fill, int* nodes, int* leaves) {
+    int lo = n, c_lo = 1, c_hi = 0;  // c_lo segments of lo points, c_hi of lo + 1
+    int nn = 0, nl = 0;
+    for (int guard = 0; guard < 40 && c_lo + c_hi > 0; ++guard) {
+        int n_lo = 0, n_hi = 0, next = 0;
+        bool have = false;
+        for (int h = 0; h < 2; ++h) {
+            const int size = lo + h, c = h ? c_hi : c_lo;
+            if (c == 0) continue;
+            if (size <= fill) {
+                nl += c;
+                continue;
+            }
+            nn += c;
+            const int a = size / 2, b = size - size / 2;  // b == a or a + 1
+            if (!have) {
+                next = a;
+                have = true;
+            }
+            // children sizes at this level are next or next + 1
+            n_lo += (a == next ? c : 0) + (b == next ? c : 0);
+            n_hi += (a == next + 1 ? c : 0) + (b == next + 1 ? c : 0);
+        }
+        lo = next;
+        c_lo = n_lo;
+        c_hi = n_hi;
+    }
+    *nodes = nn;
+    *leaves = nl;
 }
 
 template <int MAXN, int THREADS>
@@ -365,12 +402,22 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
             sm.ss[0][0] = 0;
             sm.se[0][0] = (uint16_t)n;
             sm.slink[0][0] = jb.z;
+            // The whole subtree's nodes and leaves from the pools at once
+            // (its shape follows from n and the fill); level l takes the
+            // indices after those of levels 0 .. l-1.
+            int nn = 0, nl = 0;
+            subtree_counts(n, fill, &nn, &nl);
+            sm.free_leaf_n = t.st->free_leaf_n;
+            sm.free_node_n = t.st->free_node_n;
+            sm.run_leaf = pool_reserve(&t.st->free_leaf_taken, sm.free_leaf_n, &t.st->leaf_top, nl);
+            sm.run_node = pool_reserve(&t.st->free_node_taken, sm.free_node_n, &t.st->node_top, nn);
         }
         __syncthreads();
         uint16_t(*oc)[MAXN] = sm.ord0;
         uint16_t(*on)[MAXN] = sm.u.a.ord1;
         int cb = 0;
         const int i0 = tid * PPT;
+        int leaf_base = 0, node_base = 0;  // indices of the runs taken by earlier levels
         for (int level = 0; level < 64; ++level) {
             const int S = sm.nseg[cb];
             if (S == 0) break;
@@ -400,14 +447,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
                     if (lane >= o) wi += y;
                 }
                 if (lane < THREADS / 32) sm.wsum[lane] = wi - w;
-                if (lane == 31) {
-                    sm.run_leaf = pool_reserve(&t.st->free_leaf_taken, t.st->free_leaf_n, &t.st->leaf_top,
-                                               (int)(wi & 0xffffu));
-                    sm.run_node = pool_reserve(&t.st->free_node_taken, t.st->free_node_n, &t.st->node_top,
-                                               (int)(wi >> 16));
-                }
+                if (lane == 31) sm.level_total = wi;
             }
             __syncthreads();
+            const uint32_t level_total = sm.level_total;
             if (live) {
                 const uint32_t wb = sm.wsum[warp];
                 const unsigned below = (1u << lane) - 1u;
@@ -421,8 +464,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
                 sm.saxis[sg] = -1;
                 sm.snode[sg] = -1;
                 if (is_leaf) {
-                    const int L = pool_pick(sm.run_leaf, t.free_leaf, t.st->free_leaf_n, t.leaf_cap,
-                                            (int)(wb & 0xffffu) + __popc(lm & below), t.st, ERR_POOL_LEAF);
+                    const int L = pool_pick(sm.run_leaf, t.free_leaf, sm.free_leaf_n, t.leaf_cap,
+                                            leaf_base + (int)(wb & 0xffffu) + __popc(lm & below), t.st,
+                                            ERR_POOL_LEAF);
                     sm.snode[sg] = L;
                     if (L >= 0) {
                         t.leaf_n[L] = cnt;
@@ -432,8 +476,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
                         write_child_cnt(t.ncnt, parent, side, cnt, 0);
                     }
                 } else {
-                    const int X = pool_pick(sm.run_node, t.free_node, t.st->free_node_n, t.node_cap,
-                                            (int)(wb >> 16) + __popc(nm & below), t.st, ERR_POOL);
+                    const int X = pool_pick(sm.run_node, t.free_node, sm.free_node_n, t.node_cap,
+                                            node_base + (int)(wb >> 16) + __popc(nm & below), t.st, ERR_POOL);
                     float ext[3];
                     for (int a = 0; a < 3; ++a) ext[a] = __fsub_rn(b.hi[a], b.lo[a]);
                     int axis = 0;
@@ -468,6 +512,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 4) local_build_
             }
             __syncthreads();
             if (sm.overflow) break;
+            leaf_base += (int)(level_total & 0xffffu);
+            node_base += (int)(level_total >> 16);
             // Leaves take their points; node segments mark each point's side
             // from its position in the split axis's array.
 #pragma unroll

@@ -475,7 +475,6 @@ struct Tree {
         int bound = list_cap;
         if (refit_first) {
             launch_refit(dt, aux, aux.items, &st_dev->n_items, bound, criteria(), stream);
-            launch_clear_dirty(dt, aux, bound, stream);
             if (debug_validate) check_valid("after the refit of a mutation", /*at_rest=*/false);
         }
         // The dirty list is consumed: the next update starts a fresh one.

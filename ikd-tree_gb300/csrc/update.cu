@@ -134,6 +134,8 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
     int lp = 0, expect = 0;
     if (code < 0) {
         int L = code_leaf(code);
+        // the dirty list is consumed by this refit (nothing below reads the flag)
+        a.dirty_flag[L] = 0;
         int llp = t.lparent[L];
         if (llp < 0) return;
         X = llp >> 1;
@@ -214,12 +216,6 @@ __global__ void refit_compute_kernel(DevTree t, UpdateAux a, const int* __restri
     }
 }
 
-__global__ void clear_dirty_kernel(UpdateAux a, const int* n_items) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_items || i >= a.list_cap) return;
-    int code = a.items[i];
-    if (code < 0) a.dirty_flag[code_leaf(code)] = 0;
-}
 
 // ---- rebuild jobs ----------------------------------------------------------------
 
@@ -1500,10 +1496,6 @@ void launch_refit(const DevTree& t, const UpdateAux& a, const int* items, const 
     refit_compute_kernel<<<blocks_for(max_items, 128), 128, 0, s>>>(t, a, items, n_items, c, c.fill);
 }
 
-void launch_clear_dirty(const DevTree& t, const UpdateAux& a, int max_items, cudaStream_t s) {
-    if (max_items <= 0) return;
-    clear_dirty_kernel<<<blocks_for(max_items, 256), 256, 0, s>>>(a, &t.st->n_items);
-}
 
 void launch_select_jobs(const DevTree& t, const UpdateAux& a, int max_viol, cudaStream_t s) {
     if (max_viol <= 0) return;

@@ -35,10 +35,10 @@ struct Criteria {
 // Marks / queues leaf L for refit.
 void launch_route_append(const DevTree& t, const UpdateAux& a, const float4* pts, long long n, int4* ovf_leaf_pt,
                          float4* ovf_pts, cudaStream_t s);
-// Refit from the codes in a.items[0 .. st->n_items) and record violators.
+// Refit from the codes in a.items[0 .. st->n_items) and record violators;
+// clears the dirty flags of the listed leaves.
 void launch_refit(const DevTree& t, const UpdateAux& a, const int* items, const int* n_items, int max_items,
                   const Criteria& c, cudaStream_t s);
-void launch_clear_dirty(const DevTree& t, const UpdateAux& a, int max_items, cudaStream_t s);
 // Select topmost violators as rebuild jobs (st->n_jobs = job count).
 void launch_select_jobs(const DevTree& t, const UpdateAux& a, int max_viol, cudaStream_t s);
 // Clears the criterion flags of the recorded violators without selecting jobs.
