@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstddef>
 #include <cstdlib>
@@ -608,7 +609,12 @@ struct Tree {
             return;
         }
         // Voxel downsampling.
-        op.ensure(align_up(sizeof(float) * n * stride) + ds_scratch_bytes(n) + align_up(sizeof(float4) * n) +
+        // (voxel, stored point) pairs: the stored points now plus this call's
+        // insertions.  IKDG_DS_PAIR_CAP lowers the room (tests use it to run
+        // the walking deletion that takes over when the list overflows).
+        long long pair_cap = std::min<long long>((long long)st->root_slots + n + 65536, INT_MAX / 2);
+        if (const char* e = std::getenv("IKDG_DS_PAIR_CAP")) pair_cap = std::max(1ll, std::min(pair_cap, std::atoll(e)));
+        op.ensure(align_up(sizeof(float) * n * stride) + ds_scratch_bytes(n, pair_cap) + align_up(sizeof(float4) * n) +
                       align_up(sizeof(int4) * n) + 4096,
                   stream);
         Carver c(op.p);
@@ -616,7 +622,7 @@ struct Tree {
         int4* ovf_leaf = c.take<int4>(n);
         float4* ovf_pts = c.take<float4>(n);
         DsScratch d;
-        carve_ds_scratch(op.p == nullptr ? nullptr : (char*)op.p + c.off, n, &d);
+        carve_ds_scratch(op.p == nullptr ? nullptr : (char*)op.p + c.off, n, pair_cap, &d);
         CK(cudaMemcpyAsync(raw, xyz, sizeof(float) * n * stride, cudaMemcpyHostToDevice, stream));
         launch_ds_prepare(dt, raw, stride, n, ds_size, d, stream);
         // No status read between the phases of a sub-batch: the kernels read

@@ -1065,6 +1065,7 @@ __device__ __forceinline__ long long group_first_from(const DsScratch& d, long l
 }
 
 __global__ void ds_h1_kernel(long long n, long long a, DsScratch d, DevStatus* st) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d.n_pairs = 0;  // ds_search_kernel lists its pairs afresh
     long long i = a + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (d.key[i].w) return;
@@ -1218,6 +1219,15 @@ __global__ void __launch_bounds__(128) ds_search_kernel(DevTree t, long long n, 
                 if (in_voxel_range(pc[k], fk[k], -1.f, ds) || in_voxel_range(pc[k], fk[k], 1.f, ds)) hz = true;
         }
         const unsigned hzb = __ballot_sync(0xffffffffu, hz);
+        // the pairs (voxel, slot) of this leaf's hits, for ds_delete_pairs_kernel
+        int pbase = 0;
+        if (lane == src) pbase = atomicAdd(d.n_pairs, __popc(inb));
+        pbase = __shfl_sync(0xffffffffu, pbase, src);
+        const int gsrc = __shfl_sync(0xffffffffu, g, src);
+        if (in) {
+            const int pos = pbase + __popc(inb & ((1u << lane) - 1u));
+            if (pos < d.pair_cap) d.pairs[pos] = make_int2(gsrc, L * LEAF_CAP + lane);
+        }
         // (distance, id) minimum over the hits: squared distances are >= 0, so
         // their bit patterns order like the values
         const float dd = in ? sq_dist(p.x, p.y, p.z, mx, my, mz) : __int_as_float(0x7f800000);
@@ -1439,9 +1449,25 @@ __global__ void __launch_bounds__(128) ds_fold_big_kernel(DevTree t, long long n
     }
 }
 
-// Deletes (with the downsample flag) every valid point in the boxes of the
-// groups whose fold decided so.
+// Deletes (with the downsample flag) the stored points ds_search_kernel found
+// in the boxes of the groups whose fold decided so: one thread per listed
+// (group, slot) pair, no tree walk (nothing moved since the search).
+__global__ void ds_delete_pairs_kernel(DevTree t, UpdateAux a, DsScratch d) {
+    const int np = *d.n_pairs;
+    if (np > d.pair_cap || (t.st->err & ERR_INPUT)) return;  // the list overflowed: ds_delete_kernel walks
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int2 pr = d.pairs[i];
+        if (!d.g_out[pr.x].x) continue;
+        float* w = &t.pts[pr.y].w;
+        *w = __uint_as_float(__float_as_uint(*w) | F_DEL | F_DSDEL);
+        mark_dirty(a, t.st, pr.y / LEAF_CAP);
+    }
+}
+
+// The same deletion by walking the tree from every voxel box, when the pair
+// list overflowed.
 __global__ void __launch_bounds__(128) ds_delete_kernel(DevTree t, UpdateAux a, DsScratch d) {
+    if (*d.n_pairs <= d.pair_cap) return;  // ds_delete_pairs_kernel did it
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool active = g < t.st->n_groups && !(t.st->err & ERR_INPUT) && d.g_out[g].x;
@@ -1603,8 +1629,9 @@ void launch_check_finite(const DevTree& t, const float* in, long long count, cud
     check_finite_kernel<<<blocks_for(count, 256), 256, 0, s>>>(t, in, count);
 }
 
-size_t ds_scratch_bytes(long long n) {
+size_t ds_scratch_bytes(long long n, long long pair_cap) {
     size_t b = 0;
+    b += au(sizeof(int2) * pair_cap) + au(sizeof(int));  // pairs, n_pairs
     b += 5 * au(sizeof(float4) * n);   // pts, box_lo, box_hi, mid, ins
     b += 2 * au(sizeof(int4) * n);     // key, s_key
     b += au(sizeof(float4) * n);       // s_pts
@@ -1617,7 +1644,7 @@ size_t ds_scratch_bytes(long long n) {
     return b;
 }
 
-void carve_ds_scratch(void* base, long long n, DsScratch* d) {
+void carve_ds_scratch(void* base, long long n, long long pair_cap, DsScratch* d) {
     char* p = (char*)base;
     auto take = [&](size_t bytes) {
         void* r = p;
@@ -1642,6 +1669,9 @@ void carve_ds_scratch(void* base, long long n, DsScratch* d) {
     d->g_best = (float4*)take(sizeof(float4) * n);
     d->big = (int*)take(sizeof(int) * n);
     d->n_big = (int*)take(sizeof(int));
+    d->pairs = (int2*)take(sizeof(int2) * pair_cap);
+    d->n_pairs = (int*)take(sizeof(int));
+    d->pair_cap = (int)pair_cap;
     d->temp = (void*)p;
 }
 
@@ -1669,6 +1699,7 @@ void launch_ds_fold(const DevTree& t, const UpdateAux& aux, long long n, long lo
     if (max_groups <= 0) return;
     ds_fold_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, n, a, first_id, d);
     ds_fold_big_kernel<<<DS_BIG_BLOCKS, 128, 0, s>>>(t, n, a, first_id, d);
+    ds_delete_pairs_kernel<<<SPEC_BLOCKS, 256, 0, s>>>(t, aux, d);
     ds_delete_kernel<<<blocks_for(max_groups, 128), 128, 0, s>>>(t, aux, d);
 }
 

@@ -104,10 +104,16 @@ struct DsScratch {
     float4* ins;        // [n] points to insert {x, y, z, id}
     int* big;           // [n] groups deferred to the warp fold
     int* n_big;         // [1]
+    int2* pairs;        // [pair_cap] {group, slot}: the stored points each voxel search found
+    int* n_pairs;       // [1] entries written (may pass pair_cap: then the deletion walks)
+    int pair_cap;
     void* temp;
 };
-size_t ds_scratch_bytes(long long n);
-void carve_ds_scratch(void* base, long long n, DsScratch* d);
+// pair_cap: room for the (voxel, stored point) pairs of a call's searches
+// (the stored points plus the call's insertions suffice unless float slivers
+// put points in several voxel boxes; beyond it the deletion walks the tree).
+size_t ds_scratch_bytes(long long n, long long pair_cap);
+void carve_ds_scratch(void* base, long long n, long long pair_cap, DsScratch* d);
 // Prepares keys and groups (once per batch).  st->n_groups = group count;
 // a non-finite input sets ERR_INPUT, after which the kernels below change
 // nothing.  The kernels read the group count and the sub-batch end on the

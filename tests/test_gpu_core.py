@@ -208,6 +208,22 @@ def test_downsample(ikdg_mod, ds):
     assert_knn(tree, ref, rng.uniform(-5, 5, (300, 3)).astype(np.float32), 5)
 
 
+def test_downsample_deletion_walk_when_pair_list_overflows(ikdg_mod, monkeypatch):
+    # The voxels' stored points are deleted from the (voxel, point) list the
+    # searches wrote; when that list overflows, a walk of every voxel box
+    # does it instead.  A room of 8 pairs forces the walk.
+    monkeypatch.setenv("IKDG_DS_PAIR_CAP", "8")
+    rng = np.random.default_rng(47)
+    base = rng.uniform(-4, 4, (6000, 3)).astype(np.float32)
+    tree, ref = ikdg_mod.KDTree(0.5, 0.6, 0.3), spec.SpecTree(0.3)
+    tree.Build(base)
+    ref.Build(base)
+    for it in range(3):
+        add = rng.uniform(-4, 4, (2500, 3)).astype(np.float32)
+        assert tree.Add_Points(add, True) == ref.Add_Points(add, True)
+        assert_same_valid(tree, ref)
+
+
 def test_downsample_voxel_boundaries(ikdg_mod):
     # Coordinates exactly on voxel faces and a 1-ulp neighbourhood of them.
     ds = 0.2
