@@ -67,14 +67,20 @@ def test_knn_every_list_storage(ikdg_mod, lanes):
 
 def test_snapshot_restore(ikdg_mod):
     """Map snapshot (flatten, ikd_Tree.cpp:1325-1352, as in the reference's
-    async demo) and restore by Build: the restored tree answers like the
-    original (points renumbered 0..n-1 by Build)."""
+    async demo) and restore by Build: the snapshot is the model's valid set,
+    and the restored tree answers like the original (points renumbered
+    0..n-1 by Build) and like the model restored from the same snapshot."""
     rng = np.random.default_rng(31)
     pts = rng.uniform(-20, 20, (30000, 3)).astype(np.float32)
-    a = ikdg_mod.KDTree(0.5, 0.6, 0.3)
+    a, ref = ikdg_mod.KDTree(0.5, 0.6, 0.3), spec.SpecTree(0.3)
     a.Build(pts)
-    a.Add_Points(rng.uniform(-20, 20, (5000, 3)).astype(np.float32), True)
-    a.Delete_Point_Boxes(random_boxes(rng, 20, -20, 20, 1, 6))
+    ref.Build(pts)
+    add = rng.uniform(-20, 20, (5000, 3)).astype(np.float32)
+    assert a.Add_Points(add, True) == ref.Add_Points(add, True)
+    boxes = random_boxes(rng, 20, -20, 20, 1, 6)
+    assert a.Delete_Point_Boxes(boxes) == ref.Delete_Point_Boxes(boxes)
+    # the snapshot is the model's valid set, ids included
+    assert_same_valid(a, ref)
     snap, ids = a.flatten(with_ids=True)
     b = ikdg_mod.KDTree(0.5, 0.6, 0.3)
     b.Build(snap)
@@ -86,6 +92,10 @@ def test_snapshot_restore(ikdg_mod):
     ok = ia >= 0
     # same neighbours: map b's ids back through the snapshot order
     assert np.array_equal(ids[ib[ok]], ia[ok])
+    # and the restored tree answers like the model restored from the snapshot
+    rb = spec.SpecTree(0.3)
+    rb.Build(snap)
+    assert_knn(b, rb, q, 8, 3.0)
 
 
 def random_boxes(rng, n, lo, hi, smin, smax):
