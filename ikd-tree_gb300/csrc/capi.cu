@@ -853,7 +853,8 @@ struct Tree {
             CK(cudaGetLastError());
             return;
         }
-        reset_counters();
+        // the search reports through the error bits alone
+        zero_fields(offsetof(DevStatus, err), sizeof(int));
         if (host_mode == 2 || (host_mode == 1 && all_pinned({ids, d2, xyz, cnt}))) {
             // Kernels read the queries and write the results in host memory:
             // each warp's rows leave as coalesced 16-byte spans, so the
